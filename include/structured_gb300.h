@@ -1,0 +1,143 @@
+/* structured_gb300 — C ABI of the GB300 residual / discrete-adjoint path.
+ *
+ * Drop-in for the hot path of anandpratap/structured.  The reference has no
+ * FFI; its boundary is the templated C++ class interface bound at compile
+ * time.  Each entry point below names the reference member it replaces.
+ *
+ * Conventions (all entry points):
+ *   - return int status: ST_OK (0) or a negative ST_ERR_* code; the message
+ *     of the last failure on the calling thread is st_last_error();
+ *   - the caller owns host buffers, the context owns device buffers; there is
+ *     no allocation per call after st_create (except where stated);
+ *   - one context = one device + one CUDA stream; calls on one context are
+ *     not thread safe;
+ *   - state layout is the reference's q[i][j][k]: cells i in [0,nic),
+ *     j in [0,njc), k in [0,nq), row-major FP64 (src/solver/solution.cpp:28),
+ *     nic = ni-1, njc = nj-1; nq = 4 laminar, 5 with Spalart-Allmaras
+ *     (k=4 holds rho*nu_tilde in the reference's ntrans slot,
+ *     src/solver/solution.cpp:9,43-45).
+ */
+#ifndef STRUCTURED_GB300_H
+#define STRUCTURED_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    ST_OK = 0,
+    ST_ERR_ARG = -1,          /* bad argument or size */
+    ST_ERR_CUDA = -2,         /* CUDA runtime / launch failure */
+    ST_ERR_NONFINITE = -3,    /* NaN/Inf detected in a result */
+    ST_ERR_NOCONV = -4,       /* iterative solve did not converge */
+    ST_ERR_TIMEOUT = -5,      /* bounded device wait expired */
+    ST_ERR_UNSUPPORTED = -6   /* option not built */
+};
+
+/* Boundary types, faces: src/model/bc.h:8-11 and src/model/bc.cpp:465-526. */
+enum { ST_BC_FREESTREAM = 0, ST_BC_SLIPWALL = 1, ST_BC_WALL = 2, ST_BC_OUTFLOW = 3,
+       ST_BC_PERIODIC = 4, ST_BC_ISOTHERMALWALL = 5, ST_BC_WAKE = 6 };
+enum { ST_FACE_BOTTOM = 0, ST_FACE_RIGHT = 1, ST_FACE_TOP = 2, ST_FACE_LEFT = 3 };
+enum { ST_VISC_POWER = 0, ST_VISC_SUTHERLAND = 1 };
+enum { ST_TURB_NONE = 0, ST_TURB_SA = 1 };
+
+/* One [[boundary]] table.  start/end are ghost-padded indices along the face;
+ * a negative end counts from the end as in BoundaryContainer::get_index
+ * (src/model/bc.cpp:436-457). */
+typedef struct st_bc {
+    int32_t type, face, start, end;
+    double u, v, T;
+} st_bc;
+
+/* Case setup: the [freestream], [solver], [source] keys of
+ * src/utils/config.cpp:32-87 plus the keys this project adds. */
+typedef struct st_case {
+    int32_t ni, nj;                 /* vertices */
+    int32_t order, lhs_order;       /* MUSCL order for the residual / Jacobian */
+    int32_t viscosity_law;          /* ST_VISC_* */
+    int32_t turbulence;             /* ST_TURB_* */
+    int32_t nbc;
+    int32_t plate_vertex;           /* first no-slip wall vertex (objective) */
+    double rho_inf, u_inf, v_inf, p_inf, T_inf, mu_inf, pr_inf;
+    double dpdx, dpdy;              /* [source] body force */
+    double nu_tilde_inf;            /* SA freestream nu_tilde */
+    double plate_x_end;             /* objective integrates Cf dx for x <= this */
+    const st_bc* bcs;
+} st_case;
+
+typedef struct st_ctx st_ctx;
+
+typedef struct st_solve_stats {
+    int32_t iterations;             /* Krylov iterations used */
+    int32_t converged;              /* 1 if the relative tolerance was met */
+    double residual0, residual;     /* initial / final linear residual 2-norms */
+} st_solve_stats;
+
+const char* st_last_error(void);
+int st_version(void);
+
+/* Lifecycle: replaces Mesh::setup (src/utils/mesh.cpp:392-414) — metrics
+ * (Mesh::calc_metrics, mesh.cpp:172-205), fluid model, boundary container and
+ * solution arrays.  xv, yv: vertices [ni][nj] (Mesh::xv/yv).  device < 0
+ * means the current device. */
+int st_create(const st_case* c, const double* xv, const double* yv, int device, st_ctx** out);
+int st_destroy(st_ctx* ctx);
+int st_dims(const st_ctx* ctx, int* nic, int* njc, int* nq);
+
+/* State transfer (Solution::q).  Host buffers [nic][njc][nq]. */
+int st_set_state(st_ctx* ctx, const double* q_host);
+int st_get_state(st_ctx* ctx, double* q_host);
+/* SA production multiplier beta [nic][njc] (default 1). */
+int st_set_beta(st_ctx* ctx, const double* beta_host);
+int st_get_wall_distance(st_ctx* ctx, double* d_host);
+
+/* Residual: EulerEquation::calc_residual(q, rhs, lhs)
+ * (src/model/eulerequation.h:53, eulerequation.cpp:202-232), evaluated on the
+ * context's state; lhs != 0 selects lhs_order.  rhs_host [nic][njc][nq] may be
+ * NULL to keep the result on the device. */
+int st_residual(st_ctx* ctx, int lhs, double* rhs_host);
+/* Same on caller-provided device buffers (q_dev, rhs_dev: [nic][njc][nq]);
+ * beta_dev may be NULL (beta = 1). */
+int st_residual_device(st_ctx* ctx, const double* q_dev, const double* beta_dev,
+                       double* rhs_dev, int lhs);
+
+/* Local time step: EulerEquation::calc_dt(cfl), eulerequation.cpp:237-259.
+ * dt_host [nic][njc][nq] may be NULL. */
+int st_dt(st_ctx* ctx, double cfl, double* dt_host);
+/* L2 norm of each residual component of the last st_residual
+ * (Solver::step, src/solver/solver.cpp:125-134); out[nq]. */
+int st_norms(st_ctx* ctx, double* out);
+
+/* Wall skin friction at the j=0 faces, the reference's
+ * Cf = mu_inf (du/dy - dv/dx)/q_inf (IOManager::write_surface,
+ * src/utils/io.cpp:217-226), of the current state; cf_host [nic].  J is
+ * sum Cf dx over plate faces with x <= plate_x_end. */
+int st_skin_friction(st_ctx* ctx, double* cf_host, double* J);
+
+/* Forward-mode Jacobian-vector product (dR/dQ) v + (dR/dbeta) vb on the
+ * context state; vb may be NULL.  Replaces one column sweep of ADOL-C's
+ * sparse_jac (src/solver/solver.cpp:156). */
+int st_jvp_device(st_ctx* ctx, const double* v_dev, const double* vb_dev, double* jv_dev, int lhs);
+
+/* Hand-written discrete adjoint: psi_q = (dR/dQ)^T psi, psi_b = (dR/dbeta)^T psi
+ * on the context state (no tape, face fluxes recomputed).  Either output may
+ * be NULL.  All device pointers. */
+int st_vjp_device(st_ctx* ctx, const double* psi_dev, double* out_q_dev, double* out_beta_dev, int lhs);
+/* Host-buffer variant (copies in the timed path). */
+int st_vjp(st_ctx* ctx, const double* psi_host, double* out_q_host, double* out_beta_host, int lhs);
+
+/* Diagnostics: dense FP64 FMA throughput of this device (TFLOP/s). */
+int st_probe_fp64(st_ctx* ctx, double* tflops);
+/* Device time (ms) of the last residual / VJP launch sequence, CUDA events on
+ * the context stream. */
+int st_last_kernel_ms(st_ctx* ctx, double* residual_ms, double* vjp_ms);
+/* Pointer to the context's device state / stream (for zero-copy callers). */
+int st_device_state(st_ctx* ctx, double** q_dev, double** rhs_dev, void** stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
