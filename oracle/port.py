@@ -33,6 +33,7 @@ def load():
         lib.port_destroy.argtypes = [ctypes.c_void_p]
         lib.port_metrics.argtypes = [ctypes.c_void_p, _P, _P, _P, _P]
         lib.port_residual.argtypes = [ctypes.c_void_p, _P, _P, _P, ctypes.c_int]
+        lib.port_flux_scale.argtypes = [ctypes.c_void_p, _P, _P, _P, ctypes.c_int]
         lib.port_skin_friction.argtypes = [ctypes.c_void_p, _P, _P, _P]
         lib.port_dt.argtypes = [ctypes.c_void_p, _P, ctypes.c_double, _P]
         lib.port_jvp.argtypes = [ctypes.c_void_p, _P, _P, _P, _P, _P, ctypes.c_int]
@@ -78,6 +79,13 @@ class PortCase:
         b = None if beta is None else np.ascontiguousarray(beta, dtype=np.float64)
         self.lib.port_residual(self.h, _ptr(q), _ptr(b), _ptr(rhs), self._order(lhs))
         return rhs
+
+    def flux_scale(self, q, beta=None, lhs=False):
+        q = np.ascontiguousarray(q, dtype=np.float64)
+        out = np.empty_like(q)
+        b = None if beta is None else np.ascontiguousarray(beta, dtype=np.float64)
+        self.lib.port_flux_scale(self.h, _ptr(q), _ptr(b), _ptr(out), self._order(lhs))
+        return out
 
     def skin_friction(self, q):
         q = np.ascontiguousarray(q, dtype=np.float64)

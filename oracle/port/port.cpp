@@ -580,9 +580,16 @@ T sa_source(const T& rho, const T& nut, const T& mu, double d, const T& omega, c
     return rho * (prod - dest) + (SA_CB2 / SA_SIGMA) * rho * gnut2;
 }
 
+inline void add_abs(double* scale, size_t i, const double& x) { if (scale) scale[i] += std::fabs(x); }
+inline void add_abs(double*, size_t, const Dual&) {}
+
+// scale (double evaluation only, may be null): per cell and component, the sum
+// of |face flux| over the cell's four faces (convective and viscous parts
+// separately) divided by the volume -- the magnitude the residual is a small
+// difference of, used to state per-cell relative parity errors.
 template <class T>
 void residual(const PCase& pc, const T* q, const T* beta, T* rhs, int order, Work<T>& w,
-              T* cf_wall = nullptr) {
+              T* cf_wall = nullptr, double* scale = nullptr) {
     const int nic = pc.nic, njc = pc.njc, ni = pc.ni, nj = pc.nj, nq = pc.nq;
     const double R = pc.R;
     // primvars, src/model/fluid.cpp:50-67 (shift 1,1 into the ghost-padded arrays)
@@ -606,8 +613,21 @@ void residual(const PCase& pc, const T* q, const T* beta, T* rhs, int order, Wor
     if (nq == 5) reconstruct(pc, w, w.nut, w.lchi[4], w.rchi[4], w.leta[4], w.reta[4], order);
 
     for (size_t n = 0; n < (size_t)nic * njc * nq; n++) rhs[n] = 0.0;
+    if (scale) for (size_t n = 0; n < (size_t)nic * njc * nq; n++) scale[n] = 0.0;
     roe_flux(pc, pc.nchi.data(), ni * njc, w.lchi, w.rchi, w.fchi);
     roe_flux(pc, pc.neta.data(), nic * nj, w.leta, w.reta, w.feta);
+    auto accumulate_scale = [&]() {
+        for (int i = 0; i < nic; i++)
+            for (int j = 0; j < njc; j++)
+                for (int k = 0; k < nq; k++) {
+                    size_t r = ((size_t)i * njc + j) * nq + k;
+                    add_abs(scale, r, w.feta[((size_t)i * nj + j + 1) * nq + k]);
+                    add_abs(scale, r, w.feta[((size_t)i * nj + j) * nq + k]);
+                    add_abs(scale, r, w.fchi[((size_t)(i + 1) * njc + j) * nq + k]);
+                    add_abs(scale, r, w.fchi[((size_t)i * njc + j) * nq + k]);
+                }
+    };
+    if (scale) accumulate_scale();
     for (int i = 0; i < nic; i++)
         for (int j = 0; j < njc; j++)
             for (int k = 0; k < nq; k++) {
@@ -644,6 +664,7 @@ void residual(const PCase& pc, const T* q, const T* beta, T* rhs, int order, Wor
         if (nq == 5) calc_face(pc, w.mud, w.mudbc, w.mudbe);
         viscous_flux(pc, pc.nchi.data(), ni * njc, w.gchi, w.ubc, w.vbc, w.mubc, w.kbc, w.mudbc, w.fchi);
         viscous_flux(pc, pc.neta.data(), nic * nj, w.geta, w.ube, w.vbe, w.mube, w.kbe, w.mudbe, w.feta);
+        if (scale) accumulate_scale();
         for (int i = 0; i < nic; i++)
             for (int j = 0; j < njc; j++)
                 for (int k = 1; k < nq; k++) {
@@ -678,6 +699,10 @@ void residual(const PCase& pc, const T* q, const T* beta, T* rhs, int order, Wor
     for (int i = 0; i < nic; i++)
         for (int j = 0; j < njc; j++)
             for (int k = 0; k < nq; k++) rhs[((size_t)i * njc + j) * nq + k] /= pc.VOL(i, j);
+    if (scale)
+        for (int i = 0; i < nic; i++)
+            for (int j = 0; j < njc; j++)
+                for (int k = 0; k < nq; k++) scale[((size_t)i * njc + j) * nq + k] /= pc.VOL(i, j);
 
     if (cf_wall) {
         // IOManager::write_surface, src/utils/io.cpp:217-226: the j=0 face
@@ -738,6 +763,13 @@ int port_metrics(void* hp, double* nchi, double* neta, double* vol, double* wd) 
 int port_residual(void* hp, const double* q, const double* beta, double* rhs, int order) {
     auto* h = static_cast<Handle*>(hp);
     residual<double>(h->pc, q, beta, rhs, order, h->wd);
+    return 0;
+}
+
+int port_flux_scale(void* hp, const double* q, const double* beta, double* scale, int order) {
+    auto* h = static_cast<Handle*>(hp);
+    std::vector<double> rhs((size_t)h->pc.nic * h->pc.njc * h->pc.nq);
+    residual<double>(h->pc, q, beta, rhs.data(), order, h->wd, nullptr, scale);
     return 0;
 }
 

@@ -370,3 +370,38 @@ def perturbed_state(c: Case, seed: int, amplitude: float = 0.01) -> np.ndarray:
         base = c.nu_tilde_inf_ratio * c.mu_inf / c.rho_inf
         nut = base * (1.0 + amplitude * rng.standard_normal(shape))
     return conserved_from_primitive(rho, u, v, p, nut)
+
+
+def case_to_dict(c: Case) -> dict:
+    d = dataclasses.asdict(c)
+    return d
+
+
+def case_from_dict(d: dict) -> Case:
+    d = dict(d)
+    bcs = [Boundary(**b) for b in d.pop("boundaries", [])]
+    c = Case(**d)
+    c.boundaries = bcs
+    return c
+
+
+def channel_case(workdir: str, name: str, nj: int = 101, height: float = 0.1, ni: int = 3,
+                 dx: float = 1e-3, mu: float = 1e-2, dpdx: float = -0.02592, order: int = 2) -> Case:
+    """Pressure-driven channel with periodic inflow/outflow and isothermal walls,
+    the setup of the reference's examples/laminar/channel/*.inp (3x101 grid,
+    h = 0.1, mu = 1e-2, dp/dx = -0.02592)."""
+    os.makedirs(workdir, exist_ok=True)
+    x = np.arange(ni) * dx
+    y = np.linspace(0.0, height, nj)
+    xv = np.ascontiguousarray(np.repeat(x[:, None], nj, axis=1))
+    yv = np.ascontiguousarray(np.repeat(y[None, :], ni, axis=0))
+    grid_path = os.path.join(workdir, name + ".p3d")
+    write_p3d(grid_path, Grid(xv, yv, 0))
+    T_wall = 1.0 / GAMMA
+    c = Case(grid_path=grid_path, ni=ni, nj=nj, u_inf=0.01, mu_inf=mu, pr_inf=0.7, dpdx=dpdx,
+             order=order, flux="roe", label=os.path.join(workdir, name),
+             boundaries=[Boundary("isothermalwall", "top", 1, -2, 0.0, 0.0, T_wall),
+                         Boundary("isothermalwall", "bottom", 1, -2, 0.0, 0.0, T_wall),
+                         Boundary("periodic", "left", 0, -1)])
+    write_inp(os.path.join(workdir, name + ".inp"), c)
+    return c

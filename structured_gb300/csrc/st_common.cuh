@@ -1,0 +1,136 @@
+// Shared device definitions for the structured-grid residual / adjoint path.
+//
+// Data layout in HBM (one context):
+//   q     [nic][njc][nq]        conserved state, the reference's Solution::q
+//                               (src/solver/solution.cpp:28), FP64
+//   P     [nic+2][njc+2][8]     ghost-padded primitives per cell, 64 B records
+//                               {rho,u,v,p,T,nu_tilde,mu,mu_t}; the reference
+//                               keeps the first five as separate padded arrays
+//                               (src/model/eulerequation.cpp:41-47)
+//   phi_i, phi_j [nic][njc][NQ] MUSCL limiter factor per cell and primitive
+//                               (src/model/reconstruction.cpp:85-113)
+//   geo_i [ni][njc][16], geo_j [nic][nj][16]
+//                               per-face geometry: normal (n_x,n_y), unit normal,
+//                               half length, and the Green-Gauss weights of the
+//                               face gradient of src/utils/mesh.cpp:36-131
+//   F_i [ni][njc][NQ], F_j [nic][nj][NQ]  net face fluxes (convective - viscous)
+//   G_i, G_j [..][4]            SA only: face gradient parts (u_y, v_x, nt_x, nt_y)
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace st {
+
+constexpr double GAMMA = 1.4;
+constexpr double GM1 = GAMMA - 1.0;
+constexpr double OGM1 = 1.0 / GM1;
+constexpr double THM = 2.0 / 3.0, THP = 4.0 / 3.0;   // reconstruction.h:55-56
+
+// Spalart-Allmaras (SA-noft2, negative-S~ safeguard of Allmaras et al. 2012)
+constexpr double SA_CB1 = 0.1355, SA_CB2 = 0.622, SA_SIGMA = 2.0 / 3.0, SA_KAPPA = 0.41;
+constexpr double SA_CW2 = 0.3, SA_CW3 = 2.0, SA_CV1 = 7.1, SA_CV2 = 0.7, SA_CV3 = 0.9;
+constexpr double SA_CW1 = SA_CB1 / (SA_KAPPA * SA_KAPPA) + (1.0 + SA_CB2) / SA_SIGMA;
+constexpr double SA_CV1_3 = SA_CV1 * SA_CV1 * SA_CV1;
+constexpr double SA_CW3_6 = SA_CW3 * SA_CW3 * SA_CW3 * SA_CW3 * SA_CW3 * SA_CW3;
+constexpr double PR_TURB = 0.9;
+
+// primitive record slots
+enum { P_RHO = 0, P_U, P_V, P_P, P_T, P_NUT, P_MU, P_MUT, NP = 8 };
+// geometry record slots
+enum { G_NX = 0, G_NY, G_R1, G_R2, G_AJ, G_WLX, G_WLY, G_WRX, G_WRY, G_WPX, G_WPY, G_WMX, G_WMY, NGEO = 16 };
+
+struct DevBC {
+    int type, face, start, end;
+    double u, v, T;
+};
+
+// Everything a kernel needs about the case, passed by value.
+struct DevCase {
+    int ni, nj, nic, njc, nq;
+    int viscous, sa, law, nbc;
+    double R, cp, pr, rho_inf, u_inf, v_inf, p_inf, T_inf, mu_inf, nut_inf;
+    double suth_S, eps_chi, eps_eta, dpdx, dpdy;
+    const double* vol;     // [nic][njc]
+    const double* ivol;    // [nic][njc] 1/vol
+    const double* geo_i;   // [ni][njc][NGEO]
+    const double* geo_j;   // [nic][nj][NGEO]
+    const double* wd;      // [nic][njc] wall distance
+    const double* nchi;    // [ni][njc][2] (raw normals, for BCs)
+    const double* neta;    // [nic][nj][2]
+    const DevBC* bcs;      // [nbc]
+    int* err;              // device error flag
+};
+
+__host__ __device__ inline size_t pidx(const DevCase& c, int ip, int jp) {
+    return ((size_t)ip * (c.njc + 2) + jp) * NP;
+}
+
+// ---------------------------------------------------------------------------
+// forward-mode dual number (value, tangent) for exact JVPs on the device
+// ---------------------------------------------------------------------------
+struct dual {
+    double v, d;
+    __host__ __device__ dual() {}
+    __host__ __device__ dual(double x) : v(x), d(0.0) {}
+    __host__ __device__ dual(double x, double dx) : v(x), d(dx) {}
+};
+__device__ inline dual operator+(dual a, dual b) { return dual(a.v + b.v, a.d + b.d); }
+__device__ inline dual operator-(dual a, dual b) { return dual(a.v - b.v, a.d - b.d); }
+__device__ inline dual operator-(dual a) { return dual(-a.v, -a.d); }
+__device__ inline dual operator*(dual a, dual b) { return dual(a.v * b.v, fma(a.d, b.v, a.v * b.d)); }
+__device__ inline dual operator/(dual a, dual b) {
+    double r = 1.0 / b.v, q = a.v * r;
+    return dual(q, (a.d - q * b.d) * r);
+}
+__device__ inline dual operator+(dual a, double b) { return dual(a.v + b, a.d); }
+__device__ inline dual operator+(double b, dual a) { return dual(a.v + b, a.d); }
+__device__ inline dual operator-(dual a, double b) { return dual(a.v - b, a.d); }
+__device__ inline dual operator-(double b, dual a) { return dual(b - a.v, -a.d); }
+__device__ inline dual operator*(dual a, double b) { return dual(a.v * b, a.d * b); }
+__device__ inline dual operator*(double b, dual a) { return dual(a.v * b, a.d * b); }
+__device__ inline dual operator/(dual a, double b) { double r = 1.0 / b; return dual(a.v * r, a.d * r); }
+__device__ inline bool operator>=(dual a, double b) { return a.v >= b; }
+__device__ inline bool operator>(dual a, double b) { return a.v > b; }
+__device__ inline bool operator<(dual a, double b) { return a.v < b; }
+
+__device__ inline double val(double x) { return x; }
+__device__ inline double val(dual x) { return x.v; }
+
+__device__ inline double rcp(double x) { return 1.0 / x; }
+__device__ inline double tsqrt(double x) { return ::sqrt(x); }
+__device__ inline double tfabs(double x) { return ::fabs(x); }
+__device__ inline dual rcp(dual x) { double r = 1.0 / x.v; return dual(r, -x.d * r * r); }
+__device__ inline dual tsqrt(dual x) { double s = ::sqrt(x.v); return dual(s, x.d * 0.5 / s); }
+__device__ inline dual tfabs(dual x) { return x.v < 0.0 ? -x : x; }
+__device__ inline double cbrt_(double x) { return ::cbrt(x); }
+__device__ inline dual cbrt_(dual x) { double c = ::cbrt(x.v); return dual(c, x.d * c / (3.0 * x.v)); }
+// x^(1/6) for x > 0
+__device__ inline double root6(double x) { return ::cbrt(::sqrt(x)); }
+__device__ inline dual root6(dual x) { double r = ::cbrt(::sqrt(x.v)); return dual(r, x.d * r / (6.0 * x.v)); }
+
+template <class T> __device__ inline T tmin(T a, double b) { return val(a) < b ? a : T(b); }
+
+// Laminar viscosity: power law of the reference (src/model/fluid.cpp:38-40,
+// (T/T_ref)^(2/3) evaluated as cbrt(x)^2) or Sutherland.
+template <class T>
+__device__ inline T laminar_mu(const DevCase& c, T temp) {
+    if (c.law == 1) {
+        T tr = temp * (1.0 / c.T_inf);
+        return c.mu_inf * tr * tsqrt(tr) * ((c.T_inf + c.suth_S) * rcp(temp + c.suth_S));
+    }
+    T cb = cbrt_(temp * (1.0 / c.T_inf));
+    return c.mu_inf * (cb * cb);
+}
+
+// SA eddy viscosity mu_t = rho nu_tilde f_v1(chi), chi = rho nu_tilde / mu
+template <class T>
+__device__ inline T sa_mut(T rho, T nut, T mu) {
+    T chi = rho * nut * rcp(mu);
+    T chi3 = chi * chi * chi;
+    return rho * nut * (chi3 * rcp(chi3 + SA_CV1_3));
+}
+
+// bounded mbarrier / flag spin helper limit
+constexpr int SPIN_LIMIT = 1 << 22;
+
+}  // namespace st

@@ -1,0 +1,67 @@
+// Host-side context shared by the C-ABI translation units.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/structured_gb300.h"
+#include "st_common.cuh"
+
+struct st_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    st_case c{};
+    std::vector<st_bc> bcs;
+    st::DevCase dc{};
+    int nq = 4;
+    size_t ncell = 0, npad = 0, nfi = 0, nfj = 0;
+
+    // host copies
+    std::vector<double> xv, yv, vol, nchi, neta, ds_min, wall_dx;
+
+    // device buffers (double path)
+    double *q = nullptr, *rhs = nullptr, *beta = nullptr, *P = nullptr;
+    double *phi_i = nullptr, *phi_j = nullptr, *Fi = nullptr, *Fj = nullptr, *Gi = nullptr, *Gj = nullptr;
+    double *vol_d = nullptr, *ivol_d = nullptr, *geo_i = nullptr, *geo_j = nullptr, *wd = nullptr;
+    double *nchi_d = nullptr, *neta_d = nullptr, *dsmin_d = nullptr, *dt = nullptr;
+    double *norm_part = nullptr, *norm_out = nullptr, *cf = nullptr, *wall_dx_d = nullptr;
+    st::DevBC* bcs_d = nullptr;
+    int* err_d = nullptr;
+
+    // forward-mode (dual) buffers, allocated on the first JVP call
+    st::dual *qd = nullptr, *Pd = nullptr, *phid_i = nullptr, *phid_j = nullptr;
+    st::dual *Fdi = nullptr, *Fdj = nullptr, *Gdi = nullptr, *Gdj = nullptr, *rhsd = nullptr, *betad = nullptr;
+
+    // adjoint buffers, allocated on the first VJP call
+    double *Pbar = nullptr, *w = nullptr, *srec = nullptr, *arec_i = nullptr, *arec_j = nullptr;
+    double *lrec = nullptr, *psi_tmp = nullptr, *outq_tmp = nullptr, *outb_tmp = nullptr;
+
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    float last_res_ms = 0.f, last_vjp_ms = 0.f;
+    bool have_residual = false;
+};
+
+namespace stx {
+int fail(int code, const std::string& msg);
+int cuda_fail(cudaError_t e, const char* where);
+#define ST_CUDA(call)                                                  \
+    do {                                                               \
+        cudaError_t e_ = (call);                                       \
+        if (e_ != cudaSuccess) return stx::cuda_fail(e_, #call);       \
+    } while (0)
+#define ST_LAUNCH_CHECK(where)                                         \
+    do {                                                               \
+        cudaError_t e_ = cudaGetLastError();                           \
+        if (e_ != cudaSuccess) return stx::cuda_fail(e_, where);       \
+    } while (0)
+inline unsigned grid_for(size_t n, unsigned threads = 256) {
+    size_t g = (n + threads - 1) / threads;
+    if (g < 1) g = 1;
+    if (g > (1u << 30)) g = 1u << 30;
+    return (unsigned)g;
+}
+// forward pipeline on (q -> rhs) for the double path; beta may be null
+int run_residual(st_ctx* ctx, const double* q, const double* beta, double* rhs, int order);
+int ensure_adjoint_buffers(st_ctx* ctx);
+}  // namespace stx

@@ -1,0 +1,203 @@
+"""Host-side mirror of the reference's residual / solver interface over the C ABI.
+
+``EulerEquation`` mirrors src/model/eulerequation.h:16-64 (calc_residual,
+calc_dt) for one grid block; the state lives on the GPU in the reference's
+q[i][j][k] layout.  Every call goes through libstructured_gb300.so: there is no
+CPU fallback, and a missing library or GPU raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import abi
+from . import case as C
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libstructured_gb300.so")
+_P = ctypes.POINTER(ctypes.c_double)
+_lib = None
+
+
+class StructuredError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__("%s (%s)" % (msg, abi.ERRORS.get(code, str(code))))
+        self.code = code
+
+
+def _ptr(a):
+    if a is None:
+        return None
+    if a.dtype != np.float64 or not a.flags.c_contiguous:
+        raise ValueError("arrays must be C-contiguous float64")
+    return a.ctypes.data_as(_P)
+
+
+def _vp(x):
+    return ctypes.c_void_p(int(x)) if x is not None else None
+
+
+def load_library() -> ctypes.CDLL:
+    """Loads the in-tree CUDA library; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise FileNotFoundError("%s is missing: build it with `python -c \"import __graft_entry__ as g; g.build()\"`"
+                                % LIB_PATH)
+    lib = ctypes.CDLL(LIB_PATH)
+    V, I, D = ctypes.c_void_p, ctypes.c_int, ctypes.c_double
+    sig = {
+        "st_last_error": (ctypes.c_char_p, []),
+        "st_version": (I, []),
+        "st_create": (I, [ctypes.POINTER(abi.StCase), _P, _P, I, ctypes.POINTER(V)]),
+        "st_destroy": (I, [V]),
+        "st_dims": (I, [V, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I)]),
+        "st_set_state": (I, [V, _P]),
+        "st_get_state": (I, [V, _P]),
+        "st_set_beta": (I, [V, _P]),
+        "st_get_wall_distance": (I, [V, _P]),
+        "st_residual": (I, [V, I, _P]),
+        "st_residual_device": (I, [V, V, V, V, I]),
+        "st_dt": (I, [V, D, _P]),
+        "st_norms": (I, [V, _P]),
+        "st_skin_friction": (I, [V, _P, ctypes.POINTER(D)]),
+        "st_jvp_device": (I, [V, V, V, V, I]),
+        "st_vjp_device": (I, [V, V, V, V, I]),
+        "st_vjp": (I, [V, _P, _P, _P, I]),
+        "st_probe_fp64": (I, [V, ctypes.POINTER(D)]),
+        "st_last_kernel_ms": (I, [V, ctypes.POINTER(D), ctypes.POINTER(D)]),
+        "st_device_state": (I, [V, ctypes.POINTER(V), ctypes.POINTER(V), ctypes.POINTER(V)]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _check(rc: int, what: str) -> None:
+    if rc != abi.ST_OK:
+        msg = load_library().st_last_error().decode(errors="replace")
+        raise StructuredError(rc, "%s: %s" % (what, msg))
+
+
+class EulerEquation:
+    """One grid block on one GPU (reference: Mesh::setup + EulerEquation,
+    src/utils/mesh.cpp:392-414, src/model/eulerequation.h:16-64)."""
+
+    def __init__(self, case: C.Case, xv: np.ndarray | None = None, yv: np.ndarray | None = None,
+                 device: int = -1):
+        self.lib = load_library()
+        if xv is None:
+            xv, yv = C.load_grid(case)
+        self.case = case
+        self._xv = np.ascontiguousarray(xv, dtype=np.float64)
+        self._yv = np.ascontiguousarray(yv, dtype=np.float64)
+        if self._xv.shape != (case.ni, case.nj):
+            raise ValueError("grid shape %s does not match ni, nj = %d, %d" % (self._xv.shape, case.ni, case.nj))
+        self._st, self._keep = abi.make_case_struct(case)
+        h = ctypes.c_void_p()
+        _check(self.lib.st_create(ctypes.byref(self._st), _ptr(self._xv), _ptr(self._yv), device, ctypes.byref(h)),
+               "st_create")
+        self.h = h
+        nic, njc, nq = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        self.lib.st_dims(self.h, ctypes.byref(nic), ctypes.byref(njc), ctypes.byref(nq))
+        self.nic, self.njc, self.nq = nic.value, njc.value, nq.value
+        self.shape = (self.nic, self.njc, self.nq)
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.lib.st_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- state --------------------------------------------------------------
+    def set_state(self, q: np.ndarray) -> None:
+        q = np.ascontiguousarray(q, dtype=np.float64)
+        if q.shape != self.shape:
+            raise ValueError("state shape %s != %s" % (q.shape, self.shape))
+        _check(self.lib.st_set_state(self.h, _ptr(q)), "st_set_state")
+
+    def get_state(self) -> np.ndarray:
+        q = np.empty(self.shape)
+        _check(self.lib.st_get_state(self.h, _ptr(q)), "st_get_state")
+        return q
+
+    def set_beta(self, beta: np.ndarray) -> None:
+        b = np.ascontiguousarray(beta, dtype=np.float64)
+        if b.shape != (self.nic, self.njc):
+            raise ValueError("beta shape")
+        _check(self.lib.st_set_beta(self.h, _ptr(b)), "st_set_beta")
+
+    def wall_distance(self) -> np.ndarray:
+        d = np.empty((self.nic, self.njc))
+        _check(self.lib.st_get_wall_distance(self.h, _ptr(d)), "st_get_wall_distance")
+        return d
+
+    # -- reference interface -------------------------------------------------
+    def calc_residual(self, q: np.ndarray | None = None, lhs: bool = False) -> np.ndarray:
+        """EulerEquation::calc_residual (src/model/eulerequation.cpp:202-232)."""
+        if q is not None:
+            self.set_state(q)
+        rhs = np.empty(self.shape)
+        _check(self.lib.st_residual(self.h, int(lhs), _ptr(rhs)), "st_residual")
+        return rhs
+
+    def calc_dt(self, cfl: float) -> np.ndarray:
+        """EulerEquation::calc_dt (src/model/eulerequation.cpp:237-259)."""
+        dt = np.empty(self.shape)
+        _check(self.lib.st_dt(self.h, float(cfl), _ptr(dt)), "st_dt")
+        return dt
+
+    def norms(self) -> np.ndarray:
+        out = np.empty(self.nq)
+        _check(self.lib.st_norms(self.h, _ptr(out)), "st_norms")
+        return out
+
+    def skin_friction(self):
+        cf = np.empty(self.nic)
+        J = ctypes.c_double()
+        _check(self.lib.st_skin_friction(self.h, _ptr(cf), ctypes.byref(J)), "st_skin_friction")
+        return cf, J.value
+
+    # -- device-pointer entry points (torch tensors or raw CUDA pointers) -----
+    def residual_device(self, q_ptr: int, rhs_ptr: int, beta_ptr: int | None = None, lhs: bool = False) -> None:
+        _check(self.lib.st_residual_device(self.h, _vp(q_ptr), _vp(beta_ptr), _vp(rhs_ptr), int(lhs)),
+               "st_residual_device")
+
+    def jvp_device(self, v_ptr: int, jv_ptr: int, vb_ptr: int | None = None, lhs: bool = False) -> None:
+        _check(self.lib.st_jvp_device(self.h, _vp(v_ptr), _vp(vb_ptr), _vp(jv_ptr), int(lhs)), "st_jvp_device")
+
+    def vjp_device(self, psi_ptr: int, outq_ptr: int | None, outb_ptr: int | None, lhs: bool = False) -> None:
+        _check(self.lib.st_vjp_device(self.h, _vp(psi_ptr), _vp(outq_ptr), _vp(outb_ptr), int(lhs)), "st_vjp_device")
+
+    def vjp(self, psi: np.ndarray, lhs: bool = False):
+        psi = np.ascontiguousarray(psi, dtype=np.float64)
+        oq = np.empty(self.shape)
+        ob = np.empty((self.nic, self.njc))
+        _check(self.lib.st_vjp(self.h, _ptr(psi), _ptr(oq), _ptr(ob), int(lhs)), "st_vjp")
+        return oq, ob
+
+    def device_state(self):
+        q, r, s = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
+        _check(self.lib.st_device_state(self.h, ctypes.byref(q), ctypes.byref(r), ctypes.byref(s)), "st_device_state")
+        return q.value, r.value, s.value
+
+    def probe_fp64_tflops(self) -> float:
+        t = ctypes.c_double()
+        _check(self.lib.st_probe_fp64(self.h, ctypes.byref(t)), "st_probe_fp64")
+        return t.value
+
+    def last_kernel_ms(self):
+        a, b = ctypes.c_double(), ctypes.c_double()
+        _check(self.lib.st_last_kernel_ms(self.h, ctypes.byref(a), ctypes.byref(b)), "st_last_kernel_ms")
+        return a.value, b.value

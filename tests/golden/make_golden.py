@@ -1,0 +1,69 @@
+"""Generates the golden fixtures in this folder from the reference solver's own
+residual code (anandpratap/structured src/, compiled out of tree by
+oracle/Makefile into oracle/_ref/libref_serial.so).
+
+Run from the repository root where the reference sources are mounted:
+    make -C oracle ref port && python tests/golden/make_golden.py
+Each fixture stores the grid, the case, a seeded state and the reference's
+calc_residual (both reconstruction orders), calc_dt and ghost-padded
+primitives, plus the per-cell flux scale used to state relative errors.
+"""
+from __future__ import annotations
+
+import json
+import os
+import sys
+import tempfile
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from oracle.port import PortCase  # noqa: E402
+from oracle.refcase import RefCase  # noqa: E402
+from structured_gb300 import case as C  # noqa: E402
+
+OUT = os.path.dirname(os.path.abspath(__file__))
+
+
+def cases(tmp: str):
+    yield "fp_o2", C.flat_plate_case(tmp, "fp_o2", 41, 21, 0.3, 1e6, 1e-4, 1.08, lhs_order=1), 7
+    yield "fp_o1", C.flat_plate_case(tmp, "fp_o1", 41, 21, 0.3, 1e6, 1e-4, 1.08, order=1, lhs_order=1), 7
+    yield "fp_lowre", C.flat_plate_case(tmp, "fp_lowre", 33, 17, 0.2, 2e3, 2e-3, 1.1, lhs_order=1), 11
+    yield "fp_incl", C.flat_plate_case(tmp, "fp_incl", 37, 19, 0.2, 1e5, 1e-3, 1.1, top_angle_deg=2.0, lhs_order=1), 13
+    yield "channel", C.channel_case(tmp, "channel", nj=41), 17
+    c = C.flat_plate_case(tmp, "inviscid", 33, 17, 0.5, 1e6, 1e-3, 1.1, lhs_order=1)
+    c.mu_inf = 0.0
+    c.boundaries = [C.Boundary("slipwall", "bottom", 1, -2), C.Boundary("freestream", "top", 0, -1),
+                    C.Boundary("freestream", "left", 0, -1), C.Boundary("outflow", "right", 0, -1)]
+    C.write_inp(os.path.join(tmp, "inviscid.inp"), c)
+    yield "inviscid", c, 19
+
+
+def main():
+    with tempfile.TemporaryDirectory() as tmp:
+        for name, c, seed in cases(tmp):
+            xv, yv = C.load_grid(c)
+            ref = RefCase(os.path.join(tmp, name + ".inp"))
+            q = C.perturbed_state(c, seed)
+            if name == "channel":
+                q = C.perturbed_state(c, seed, amplitude=0.01)
+            rhs = ref.residual(q)
+            prim = ref.primitives()
+            rhs_lhs = ref.residual(q, lhs=True)
+            dt = ref.dt(q, 2.5)
+            port = PortCase(c, xv, yv)
+            scale = port.flux_scale(q)
+            scale_lhs = port.flux_scale(q, lhs=True)
+            d = C.case_to_dict(c)
+            d["grid_path"] = ""
+            d["label"] = name
+            np.savez_compressed(os.path.join(OUT, name + ".npz"), case=json.dumps(d), xv=xv, yv=yv, q=q,
+                                rhs=rhs, rhs_lhs=rhs_lhs, dt=dt, cfl=2.5, prim=prim, scale=scale,
+                                scale_lhs=scale_lhs, seed=seed)
+            print(name, q.shape, float(np.abs(rhs).max()))
+
+
+if __name__ == "__main__":
+    main()
