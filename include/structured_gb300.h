@@ -131,8 +131,14 @@ int st_vjp(st_ctx* ctx, const double* psi_host, double* out_q_host, double* out_
 
 /* Diagnostics: dense FP64 FMA throughput of this device (TFLOP/s). */
 int st_probe_fp64(st_ctx* ctx, double* tflops);
+/* Runs the residual pipeline once on the context state with a CUDA event
+ * between launches: ms[k] is the device time of launch k, *nkernels the count
+ * (at most 8).  Order: primitives, boundary conditions, limiter, i-faces,
+ * j-faces, cell assembly. */
+int st_profile_residual(st_ctx* ctx, int lhs, double* ms, int* nkernels);
 /* Device time (ms) of the last residual / VJP launch sequence, CUDA events on
- * the context stream. */
+ * the context stream (waits for them).  The *_device entry points are
+ * asynchronous on the context stream; the host-buffer ones synchronise. */
 int st_last_kernel_ms(st_ctx* ctx, double* residual_ms, double* vjp_ms);
 /* Pointer to the context's device state / stream (for zero-copy callers). */
 int st_device_state(st_ctx* ctx, double** q_dev, double** rhs_dev, void** stream);

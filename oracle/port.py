@@ -31,6 +31,8 @@ def load():
         lib.port_create.restype = ctypes.c_void_p
         lib.port_create.argtypes = [ctypes.POINTER(abi.StCase), _P, _P]
         lib.port_destroy.argtypes = [ctypes.c_void_p]
+        lib.port_set_threads.argtypes = [ctypes.c_int]
+        lib.port_set_threads.restype = ctypes.c_int
         lib.port_metrics.argtypes = [ctypes.c_void_p, _P, _P, _P, _P]
         lib.port_residual.argtypes = [ctypes.c_void_p, _P, _P, _P, ctypes.c_int]
         lib.port_flux_scale.argtypes = [ctypes.c_void_p, _P, _P, _P, ctypes.c_int]
@@ -63,6 +65,9 @@ class PortCase:
                 self.h = None
         except Exception:
             pass
+
+    def set_threads(self, n: int) -> int:
+        return self.lib.port_set_threads(n)
 
     def _order(self, lhs):
         return self.case.lhs_order if (lhs and self.case.lhs_order) else self.case.order

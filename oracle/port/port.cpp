@@ -25,6 +25,9 @@
 
 #include <algorithm>
 #include <cmath>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 #include <cstring>
 #include <vector>
 
@@ -316,11 +319,13 @@ void reconstruct(const PCase& pc, const Work<T>& w, const std::vector<T>& q,
     const int ni = pc.ni, nj = pc.nj, nic = pc.nic, njc = pc.njc;
     const double thm = 2.0 / 3.0, thp = 4.0 / 3.0;
     auto Q = [&](int i, int j) -> const T& { return q[(size_t)i * (njc + 2) + j]; };
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < ni; i++)
         for (int j = 0; j < njc; j++) {
             lchi[(size_t)i * njc + j] = Q(i, j + 1);
             rchi[(size_t)i * njc + j] = Q(i + 1, j + 1);
         }
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < nic; i++)
         for (int j = 0; j < nj; j++) {
             leta[(size_t)i * nj + j] = Q(i + 1, j);
@@ -330,8 +335,10 @@ void reconstruct(const PCase& pc, const Work<T>& w, const std::vector<T>& q,
     {
         const double eps = pc.eps_chi;
         std::vector<T> f2((size_t)ni * njc);
+#pragma omp parallel for schedule(static)
         for (int i = 0; i < ni; i++)
             for (int j = 0; j < njc; j++) f2[(size_t)i * njc + j] = Q(i + 1, j + 1) - Q(i, j + 1);
+#pragma omp parallel for schedule(static)
         for (int i = 0; i < nic; i++)
             for (int j = 0; j < njc; j++) {
                 const T& fa = f2[(size_t)i * njc + j];
@@ -346,8 +353,10 @@ void reconstruct(const PCase& pc, const Work<T>& w, const std::vector<T>& q,
     {
         const double eps = pc.eps_eta;
         std::vector<T> f2((size_t)nic * nj);
+#pragma omp parallel for schedule(static)
         for (int i = 0; i < nic; i++)
             for (int j = 0; j < nj; j++) f2[(size_t)i * nj + j] = Q(i + 1, j + 1) - Q(i + 1, j);
+#pragma omp parallel for schedule(static)
         for (int i = 0; i < nic; i++)
             for (int j = 0; j < njc; j++) {
                 const T& fa = f2[(size_t)i * nj + j];
@@ -460,6 +469,7 @@ void roe_flux(const PCase& pc, const double* normal, int nfaces,
     constexpr double gm1 = GAMMA - 1.0;
     constexpr double ogm1 = 1.0 / gm1;
     const int nq = pc.nq;
+#pragma omp parallel for schedule(static)
     for (int idx = 0; idx < nfaces; idx++) {
         const double nx = normal[idx * 2 + 0], ny = normal[idx * 2 + 1];
         const T rlft = L[0][idx], ulft = L[1][idx], vlft = L[2][idx], plft = L[3][idx];
@@ -592,7 +602,11 @@ void residual(const PCase& pc, const T* q, const T* beta, T* rhs, int order, Wor
               T* cf_wall = nullptr, double* scale = nullptr) {
     const int nic = pc.nic, njc = pc.njc, ni = pc.ni, nj = pc.nj, nq = pc.nq;
     const double R = pc.R;
-    // primvars, src/model/fluid.cpp:50-67 (shift 1,1 into the ghost-padded arrays)
+    // primvars, src/model/fluid.cpp:50-67 (shift 1,1 into the ghost-padded arrays).
+    // OpenMP pragmas sit on the loops the reference parallelises
+    // (fluid.cpp:53, reconstruction.cpp:30-107, flux.cpp:60, eulerequation.cpp:145,227)
+    // and on this project's cell-local SA loops.
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < nic; i++)
         for (int j = 0; j < njc; j++) {
             const T* Q = &q[((size_t)i * njc + j) * nq];
@@ -616,6 +630,14 @@ void residual(const PCase& pc, const T* q, const T* beta, T* rhs, int order, Wor
     if (scale) for (size_t n = 0; n < (size_t)nic * njc * nq; n++) scale[n] = 0.0;
     roe_flux(pc, pc.nchi.data(), ni * njc, w.lchi, w.rchi, w.fchi);
     roe_flux(pc, pc.neta.data(), nic * nj, w.leta, w.reta, w.feta);
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < nic; i++)
+        for (int j = 0; j < njc; j++)
+            for (int k = 0; k < nq; k++) {
+                T& r = rhs[((size_t)i * njc + j) * nq + k];
+                r -= (w.feta[((size_t)i * nj + j + 1) * nq + k] - w.feta[((size_t)i * nj + j) * nq + k]);
+                r -= (w.fchi[((size_t)(i + 1) * njc + j) * nq + k] - w.fchi[((size_t)i * njc + j) * nq + k]);
+            }
     auto accumulate_scale = [&]() {
         for (int i = 0; i < nic; i++)
             for (int j = 0; j < njc; j++)
@@ -628,13 +650,6 @@ void residual(const PCase& pc, const T* q, const T* beta, T* rhs, int order, Wor
                 }
     };
     if (scale) accumulate_scale();
-    for (int i = 0; i < nic; i++)
-        for (int j = 0; j < njc; j++)
-            for (int k = 0; k < nq; k++) {
-                T& r = rhs[((size_t)i * njc + j) * nq + k];
-                r -= (w.feta[((size_t)i * nj + j + 1) * nq + k] - w.feta[((size_t)i * nj + j) * nq + k]);
-                r -= (w.fchi[((size_t)(i + 1) * njc + j) * nq + k] - w.fchi[((size_t)i * njc + j) * nq + k]);
-            }
     if (pc.viscous) {
         for (int g = 0; g < w.np; g++) {
             T mu = laminar_mu(pc, w.T_[g]);
@@ -673,6 +688,7 @@ void residual(const PCase& pc, const T* q, const T* beta, T* rhs, int order, Wor
                     r += (w.fchi[((size_t)(i + 1) * njc + j) * nq + k] - w.fchi[((size_t)i * njc + j) * nq + k]);
                 }
         if (nq == 5) {
+#pragma omp parallel for schedule(static)
             for (int i = 0; i < nic; i++)
                 for (int j = 0; j < njc; j++) {
                     auto cg = [&](int m, int k) {
@@ -696,6 +712,7 @@ void residual(const PCase& pc, const T* q, const T* beta, T* rhs, int order, Wor
             rhs[((size_t)i * njc + j) * nq + 1] += -pc.c.dpdx * pc.VOL(i, j);
             rhs[((size_t)i * njc + j) * nq + 2] += -pc.c.dpdy * pc.VOL(i, j);
         }
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < nic; i++)
         for (int j = 0; j < njc; j++)
             for (int k = 0; k < nq; k++) rhs[((size_t)i * njc + j) * nq + k] /= pc.VOL(i, j);
@@ -750,6 +767,16 @@ void* port_create(const st_case* c, const double* xv, const double* yv) {
 }
 
 void port_destroy(void* h) { delete static_cast<Handle*>(h); }
+
+int port_set_threads(int n) {
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+    return omp_get_max_threads();
+#else
+    (void)n;
+    return 1;
+#endif
+}
 
 int port_metrics(void* hp, double* nchi, double* neta, double* vol, double* wd) {
     auto* h = static_cast<Handle*>(hp);

@@ -316,12 +316,16 @@ def flat_plate_boundaries(i_le: int, top: str = "freestream") -> list:
 def flat_plate_case(workdir: str, name: str, ni: int, nj: int, mach: float, reynolds: float,
                     h1: float, ratio: float, y_max: float = 0.5, x_min: float = -0.25,
                     x_max: float = 1.0, top_angle_deg: float = 0.0, turbulence: str = "none",
-                    pr: float = 0.72, viscosity_law: str = "power", **solver) -> Case:
-    """Writes grid + ``.inp`` for one flat-plate workload and returns the Case."""
-    os.makedirs(workdir, exist_ok=True)
+                    pr: float = 0.72, viscosity_law: str = "power", write_files: bool = True,
+                    **solver) -> Case:
+    """Writes grid + ``.inp`` for one flat-plate workload and returns the Case.
+    With write_files=False nothing is written; the grid is then regenerated
+    by flat_plate_grid() with the same arguments."""
     grid = flat_plate_grid(ni, nj, x_min, x_max, y_max, h1, ratio, top_angle_deg)
     grid_path = os.path.join(workdir, name + ".p3d")
-    write_p3d(grid_path, grid)
+    if write_files:
+        os.makedirs(workdir, exist_ok=True)
+        write_p3d(grid_path, grid)
     top = "freestream" if abs(top_angle_deg) < 1e-12 else "slipwall"
     c = Case(grid_path=grid_path, ni=ni, nj=nj, u_inf=float(mach), mu_inf=float(mach / reynolds),
              pr_inf=pr, flux="roe", boundaries=flat_plate_boundaries(grid.i_le, top),
@@ -329,7 +333,8 @@ def flat_plate_case(workdir: str, name: str, ni: int, nj: int, mach: float, reyn
              label=os.path.join(workdir, name))
     for k, v in solver.items():
         setattr(c, k, v)
-    write_inp(os.path.join(workdir, name + ".inp"), c)
+    if write_files:
+        write_inp(os.path.join(workdir, name + ".inp"), c)
     return c
 
 

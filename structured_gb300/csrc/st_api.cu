@@ -324,7 +324,7 @@ int st_version(void) { return 1; }
 
 int st_create(const st_case* c, const double* xv, const double* yv, int device, st_ctx** out) {
     if (!c || !xv || !yv || !out) return fail(ST_ERR_ARG, "st_create: null argument");
-    if (c->ni < 4 || c->nj < 4) return fail(ST_ERR_ARG, "st_create: grid must have ni, nj >= 4");
+    if (c->ni < 3 || c->nj < 3) return fail(ST_ERR_ARG, "st_create: grid must have ni, nj >= 3");
     if (c->order != 1 && c->order != 2) return fail(ST_ERR_ARG, "st_create: order must be 1 or 2");
     if (c->lhs_order != 1 && c->lhs_order != 2) return fail(ST_ERR_ARG, "st_create: lhs_order must be 1 or 2");
     if (c->nbc < 0 || (c->nbc > 0 && !c->bcs)) return fail(ST_ERR_ARG, "st_create: bad boundary list");
@@ -514,8 +514,7 @@ int st_residual_device(st_ctx* x, const double* q_dev, const double* beta_dev, d
     int rc = stx::run_residual(x, q_dev, beta_dev, rhs_dev, order_of(x, lhs));
     if (rc) return rc;
     cudaEventRecord(x->ev[1], x->stream);
-    ST_CUDA(cudaEventSynchronize(x->ev[1]));
-    cudaEventElapsedTime(&x->last_res_ms, x->ev[0], x->ev[1]);
+    x->res_pending = true;
     return ST_OK;
 }
 
@@ -524,10 +523,8 @@ int st_residual(st_ctx* x, int lhs, double* rhs_host) {
     int rc = st_residual_device(x, x->q, x->beta, x->rhs, lhs);
     if (rc) return rc;
     x->have_residual = true;
-    if (rhs_host) {
-        ST_CUDA(cudaMemcpyAsync(rhs_host, x->rhs, x->ncell * x->nq * 8, cudaMemcpyDeviceToHost, x->stream));
-        ST_CUDA(cudaStreamSynchronize(x->stream));
-    }
+    if (rhs_host) ST_CUDA(cudaMemcpyAsync(rhs_host, x->rhs, x->ncell * x->nq * 8, cudaMemcpyDeviceToHost, x->stream));
+    ST_CUDA(cudaStreamSynchronize(x->stream));
     return ST_OK;
 }
 
@@ -625,19 +622,77 @@ int st_probe_fp64(st_ctx* x, double* tflops) {
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, x->device);
     const int blocks = sms * 2, threads = 256, iters = 4096;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
     k_dfma_probe<<<blocks, threads, 0, x->stream>>>(x->norm_out, 16, 0.999, 1e-3);
-    cudaEventRecord(x->ev[2], x->stream);
+    cudaEventRecord(e0, x->stream);
     k_dfma_probe<<<blocks, threads, 0, x->stream>>>(x->norm_out, iters, 0.999, 1e-3);
-    cudaEventRecord(x->ev[3], x->stream);
-    ST_CUDA(cudaEventSynchronize(x->ev[3]));
+    cudaEventRecord(e1, x->stream);
+    cudaError_t err = cudaEventSynchronize(e1);
     float ms = 0.f;
-    cudaEventElapsedTime(&ms, x->ev[2], x->ev[3]);
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (err != cudaSuccess) return stx::cuda_fail(err, "st_probe_fp64");
     *tflops = 2.0 * blocks * threads * (double)iters * 8 / (ms * 1e-3) / 1e12;
+    return ST_OK;
+}
+
+// Runs the residual pipeline once on the context state with an event
+// between kernels; ms[k] = device time of launch k (at most 8 entries).
+int st_profile_residual(st_ctx* x, int lhs, double* ms, int* nkernels) {
+    if (!x || !ms || !nkernels) return fail(ST_ERR_ARG, "st_profile_residual: null argument");
+    cudaEvent_t ev[8];
+    for (auto& e : ev) cudaEventCreate(&e);
+    cudaStream_t s = x->stream;
+    const DevCase& dc = x->dc;
+    const int order = order_of(x, lhs);
+    const unsigned gc = grid_for(x->ncell);
+    int n = 0;
+    cudaEventRecord(ev[n++], s);
+#define PROF_PIPE(NQ)                                                                                  \
+    k_prim<double, NQ><<<gc, 256, 0, s>>>(dc, x->q, x->P); cudaEventRecord(ev[n++], s);                \
+    k_bc<double, NQ><<<1, 1024, 0, s>>>(dc, x->P); cudaEventRecord(ev[n++], s);                         \
+    k_limiter<double, NQ><<<gc, 256, 0, s>>>(dc, x->P, x->phi_i, x->phi_j); cudaEventRecord(ev[n++], s); \
+    if (order == 2) {                                                                                  \
+        k_face<double, NQ, 0, 2><<<grid_for(x->nfi), 256, 0, s>>>(dc, x->P, x->phi_i, x->Fi, x->Gi);     \
+        cudaEventRecord(ev[n++], s);                                                                   \
+        k_face<double, NQ, 1, 2><<<grid_for(x->nfj), 256, 0, s>>>(dc, x->P, x->phi_j, x->Fj, x->Gj);     \
+    } else {                                                                                           \
+        k_face<double, NQ, 0, 1><<<grid_for(x->nfi), 256, 0, s>>>(dc, x->P, x->phi_i, x->Fi, x->Gi);     \
+        cudaEventRecord(ev[n++], s);                                                                   \
+        k_face<double, NQ, 1, 1><<<grid_for(x->nfj), 256, 0, s>>>(dc, x->P, x->phi_j, x->Fj, x->Gj);     \
+    }                                                                                                  \
+    cudaEventRecord(ev[n++], s);                                                                       \
+    k_cell<double, NQ><<<gc, 256, 0, s>>>(dc, x->P, x->Fi, x->Fj, x->Gi, x->Gj, x->beta, x->rhs);        \
+    cudaEventRecord(ev[n++], s);
+    if (x->nq == 5) { PROF_PIPE(5) } else { PROF_PIPE(4) }
+#undef PROF_PIPE
+    cudaError_t e = cudaEventSynchronize(ev[n - 1]);
+    for (int k = 0; k + 1 < n; k++) {
+        float t = 0.f;
+        cudaEventElapsedTime(&t, ev[k], ev[k + 1]);
+        ms[k] = t;
+    }
+    *nkernels = n - 1;
+    for (auto& ee : ev) cudaEventDestroy(ee);
+    if (e != cudaSuccess) return stx::cuda_fail(e, "st_profile_residual");
     return ST_OK;
 }
 
 int st_last_kernel_ms(st_ctx* x, double* res_ms, double* vjp_ms) {
     if (!x) return fail(ST_ERR_ARG, "st_last_kernel_ms: null context");
+    if (x->res_pending) {
+        ST_CUDA(cudaEventSynchronize(x->ev[1]));
+        cudaEventElapsedTime(&x->last_res_ms, x->ev[0], x->ev[1]);
+        x->res_pending = false;
+    }
+    if (x->vjp_pending) {
+        ST_CUDA(cudaEventSynchronize(x->ev[3]));
+        cudaEventElapsedTime(&x->last_vjp_ms, x->ev[2], x->ev[3]);
+        x->vjp_pending = false;
+    }
     if (res_ms) *res_ms = x->last_res_ms;
     if (vjp_ms) *vjp_ms = x->last_vjp_ms;
     return ST_OK;

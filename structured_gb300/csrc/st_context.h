@@ -40,6 +40,7 @@ struct st_ctx {
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     float last_res_ms = 0.f, last_vjp_ms = 0.f;
     bool have_residual = false;
+    bool res_pending = false, vjp_pending = false;
 };
 
 namespace stx {

@@ -69,6 +69,7 @@ def load_library() -> ctypes.CDLL:
         "st_vjp": (I, [V, _P, _P, _P, I]),
         "st_probe_fp64": (I, [V, ctypes.POINTER(D)]),
         "st_last_kernel_ms": (I, [V, ctypes.POINTER(D), ctypes.POINTER(D)]),
+        "st_profile_residual": (I, [V, I, _P, ctypes.POINTER(I)]),
         "st_device_state": (I, [V, ctypes.POINTER(V), ctypes.POINTER(V), ctypes.POINTER(V)]),
     }
     for name, (res, args) in sig.items():
@@ -196,6 +197,12 @@ class EulerEquation:
         t = ctypes.c_double()
         _check(self.lib.st_probe_fp64(self.h, ctypes.byref(t)), "st_probe_fp64")
         return t.value
+
+    def profile_residual(self, lhs: bool = False):
+        ms = np.zeros(8)
+        n = ctypes.c_int()
+        _check(self.lib.st_profile_residual(self.h, int(lhs), _ptr(ms), ctypes.byref(n)), "st_profile_residual")
+        return ms[:n.value]
 
     def last_kernel_ms(self):
         a, b = ctypes.c_double(), ctypes.c_double()
