@@ -239,7 +239,8 @@ def run_ours(args, world, rank, local):
         torch.cuda.synchronize()
     except StructuredError:
         with_adj = False
-    kernels_per_step = 6 + (eq.vjp_kernel_count() if with_adj else 0)
+    n_res, n_vjp = eq.launch_counts()
+    kernels_per_step = n_res + (n_vjp if with_adj else 0)
 
     def step():
         eq.residual_device(qd, rd)

@@ -129,6 +129,9 @@ int st_vjp_device(st_ctx* ctx, const double* psi_dev, double* out_q_dev, double*
 /* Host-buffer variant (copies in the timed path). */
 int st_vjp(st_ctx* ctx, const double* psi_host, double* out_q_host, double* out_beta_host, int lhs);
 
+/* Kernel launches one st_residual_device / st_vjp_device call makes. */
+int st_launch_counts(st_ctx* ctx, int lhs, int* residual, int* vjp);
+
 /* Diagnostics: dense FP64 FMA throughput of this device (TFLOP/s). */
 int st_probe_fp64(st_ctx* ctx, double* tflops);
 /* Runs the residual pipeline once on the context state with a CUDA event

@@ -1,14 +1,114 @@
-// Hand-written discrete adjoint (reverse mode) of the residual pipeline.
+// C ABI of the hand-written discrete adjoint: launch sequence of the reverse
+// passes in st_adjoint.cuh.
+#include <algorithm>
+
+#include "st_adjoint.cuh"
 #include "st_context.h"
-#include "st_kernels.cuh"
+
+using namespace st;
+using stx::fail;
+using stx::grid_for;
+
+namespace {
+
+template <class T>
+int alloc_d(T** p, size_t n) {
+    cudaError_t e = cudaMalloc((void**)p, std::max<size_t>(n, 1) * sizeof(T));
+    if (e != cudaSuccess) return stx::cuda_fail(e, "cudaMalloc (adjoint buffers)");
+    return ST_OK;
+}
+
+int ensure(st_ctx* x) {
+    if (x->Pbar) return ST_OK;
+    const int nq = x->nq;
+    const size_t ring = 2 * (size_t)(x->c.ni + 1) + 2 * (size_t)(x->c.nj - 1);
+    int rc = ST_OK;
+    if (rc == ST_OK) rc = alloc_d(&x->Pbar, x->npad * NP);
+    if (rc == ST_OK) rc = alloc_d(&x->w, x->ncell * nq);
+    if (rc == ST_OK) rc = alloc_d(&x->srec, x->ncell * SRW);
+    if (rc == ST_OK) rc = alloc_d(&x->arec_i, x->nfi * ARW);
+    if (rc == ST_OK) rc = alloc_d(&x->arec_j, x->nfj * ARW);
+    if (rc == ST_OK) rc = alloc_d(&x->lrec, x->ncell * 4 * nq);
+    if (rc == ST_OK) rc = alloc_d(&x->tape, std::max(1, x->c.nbc) * ring * RW);
+    if (rc == ST_OK) rc = alloc_d(&x->psi_tmp, x->ncell * nq);
+    if (rc == ST_OK) rc = alloc_d(&x->outq_tmp, x->ncell * nq);
+    if (rc == ST_OK) rc = alloc_d(&x->outb_tmp, x->ncell);
+    if (rc) return rc;
+    ST_CUDA(cudaMemsetAsync(x->srec, 0, x->ncell * SRW * 8, x->stream));
+    return ST_OK;
+}
+
+template <int NQ, int ORDER>
+int launch_vjp(st_ctx* x, const double* psi, double* outq, double* outb) {
+    cudaStream_t s = x->stream;
+    const DevCase& dc = x->dc;
+    const unsigned gc = grid_for(x->ncell);
+    k_prim<double, NQ><<<gc, 256, 0, s>>>(dc, x->q, x->P);
+    k_bc_taped<NQ><<<1, 1024, 0, s>>>(dc, x->P, x->tape);
+    if (ORDER == 2) k_limiter<double, NQ><<<gc, 256, 0, s>>>(dc, x->P, x->phi_i, x->phi_j);
+    if (NQ == 5 && dc.viscous) {
+        k_face_grad<0><<<grid_for(x->nfi), 256, 0, s>>>(dc, x->P, x->Gi);
+        k_face_grad<1><<<grid_for(x->nfj), 256, 0, s>>>(dc, x->P, x->Gj);
+    }
+    k_cell_adj<NQ><<<gc, 256, 0, s>>>(dc, x->P, x->Gi, x->Gj, x->beta, psi, x->w, x->srec, outb);
+    k_face_adj<NQ, 0, ORDER><<<grid_for(x->nfi), 256, 0, s>>>(dc, x->P, x->phi_i, x->w, x->srec, x->arec_i);
+    k_face_adj<NQ, 1, ORDER><<<grid_for(x->nfj), 256, 0, s>>>(dc, x->P, x->phi_j, x->w, x->srec, x->arec_j);
+    if (ORDER == 2)
+        k_limiter_adj<NQ><<<gc, 256, 0, s>>>(dc, x->P, x->phi_i, x->phi_j, x->arec_i, x->arec_j, x->lrec);
+    k_gather<NQ, ORDER><<<grid_for(x->npad), 256, 0, s>>>(dc, x->P, x->arec_i, x->arec_j, x->lrec, x->srec, x->Pbar);
+    k_bc_adj<NQ><<<1, 1024, 0, s>>>(dc, x->P, x->tape, x->Pbar);
+    k_prim_adj<NQ><<<gc, 256, 0, s>>>(dc, x->q, x->P, x->Pbar, outq);
+    ST_LAUNCH_CHECK("vjp launch");
+    return ST_OK;
+}
+
+int vjp_launches(const st_ctx* x, int order) {
+    int n = 8;  // prim, bc, cell_adj, face_adj x2, gather, bc_adj, prim_adj
+    if (order == 2) n += 2;  // limiter, limiter_adj
+    if (x->nq == 5 && x->dc.viscous) n += 2;  // face gradient parts
+    return n;
+}
+
+}  // namespace
 
 extern "C" {
-int st_vjp_device(st_ctx* x, const double*, double*, double*, int) {
-    if (!x) return stx::fail(ST_ERR_ARG, "st_vjp_device: null context");
-    return stx::fail(ST_ERR_UNSUPPORTED, "st_vjp_device: not built yet");
+
+int st_vjp_device(st_ctx* x, const double* psi, double* outq, double* outb, int lhs) {
+    if (!x || !psi) return fail(ST_ERR_ARG, "st_vjp_device: null argument");
+    int rc = ensure(x);
+    if (rc) return rc;
+    const int order = lhs ? x->c.lhs_order : x->c.order;
+    double* oq = outq ? outq : x->outq_tmp;
+    double* ob = outb ? outb : x->outb_tmp;
+    if (x->nq == 4) ST_CUDA(cudaMemsetAsync(ob, 0, x->ncell * 8, x->stream));
+    cudaEventRecord(x->ev[2], x->stream);
+    if (x->nq == 5) rc = order == 2 ? launch_vjp<5, 2>(x, psi, oq, ob) : launch_vjp<5, 1>(x, psi, oq, ob);
+    else rc = order == 2 ? launch_vjp<4, 2>(x, psi, oq, ob) : launch_vjp<4, 1>(x, psi, oq, ob);
+    if (rc) return rc;
+    cudaEventRecord(x->ev[3], x->stream);
+    x->vjp_pending = true;
+    return ST_OK;
 }
-int st_vjp(st_ctx* x, const double*, double*, double*, int) {
-    if (!x) return stx::fail(ST_ERR_ARG, "st_vjp: null context");
-    return stx::fail(ST_ERR_UNSUPPORTED, "st_vjp: not built yet");
+
+int st_vjp(st_ctx* x, const double* psi_host, double* outq_host, double* outb_host, int lhs) {
+    if (!x || !psi_host) return fail(ST_ERR_ARG, "st_vjp: null argument");
+    int rc = ensure(x);
+    if (rc) return rc;
+    ST_CUDA(cudaMemcpyAsync(x->psi_tmp, psi_host, x->ncell * x->nq * 8, cudaMemcpyHostToDevice, x->stream));
+    rc = st_vjp_device(x, x->psi_tmp, x->outq_tmp, x->outb_tmp, lhs);
+    if (rc) return rc;
+    if (outq_host) ST_CUDA(cudaMemcpyAsync(outq_host, x->outq_tmp, x->ncell * x->nq * 8, cudaMemcpyDeviceToHost, x->stream));
+    if (outb_host) ST_CUDA(cudaMemcpyAsync(outb_host, x->outb_tmp, x->ncell * 8, cudaMemcpyDeviceToHost, x->stream));
+    ST_CUDA(cudaStreamSynchronize(x->stream));
+    return ST_OK;
 }
+
+int st_launch_counts(st_ctx* x, int lhs, int* residual, int* vjp) {
+    if (!x) return fail(ST_ERR_ARG, "st_launch_counts: null context");
+    const int order = lhs ? x->c.lhs_order : x->c.order;
+    if (residual) *residual = order == 2 ? 6 : 5;
+    if (vjp) *vjp = vjp_launches(x, order);
+    return ST_OK;
 }
+
+}  // extern "C"

@@ -289,8 +289,8 @@ int launch_forward(st_ctx* x, const DevCase& dc, const T* q, const T* beta, T* P
     const unsigned gc = grid_for(x->ncell);
     k_prim<T, NQ><<<gc, 256, 0, s>>>(dc, q, P);
     k_bc<T, NQ><<<1, 1024, 0, s>>>(dc, P);
-    if (order == 2) k_limiter<T, NQ><<<gc, 256, 0, s>>>(dc, P, phi_i, phi_j);
     if (order == 2) {
+        k_limiter<T, NQ><<<gc, 256, 0, s>>>(dc, P, phi_i, phi_j);
         k_face<T, NQ, 0, 2><<<grid_for(x->nfi), 256, 0, s>>>(dc, P, phi_i, Fi, Gi);
         k_face<T, NQ, 1, 2><<<grid_for(x->nfj), 256, 0, s>>>(dc, P, phi_j, Fj, Gj);
     } else {
@@ -460,7 +460,7 @@ int st_destroy(st_ctx* x) {
     double* bufs[] = {x->q, x->rhs, x->beta, x->P, x->phi_i, x->phi_j, x->Fi, x->Fj, x->Gi, x->Gj, x->vol_d, x->ivol_d,
                       x->geo_i, x->geo_j, x->wd, x->nchi_d, x->neta_d, x->dsmin_d, x->dt, x->norm_part, x->norm_out,
                       x->cf, x->wall_dx_d, x->Pbar, x->w, x->srec, x->arec_i, x->arec_j, x->lrec, x->psi_tmp,
-                      x->outq_tmp, x->outb_tmp};
+                      x->outq_tmp, x->outb_tmp, x->tape};
     for (double* b : bufs) if (b) cudaFree(b);
     st::dual* dbufs[] = {x->qd, x->Pd, x->phid_i, x->phid_j, x->Fdi, x->Fdj, x->Gdi, x->Gdj, x->rhsd, x->betad};
     for (st::dual* b : dbufs) if (b) cudaFree(b);

@@ -35,7 +35,7 @@ struct st_ctx {
 
     // adjoint buffers, allocated on the first VJP call
     double *Pbar = nullptr, *w = nullptr, *srec = nullptr, *arec_i = nullptr, *arec_j = nullptr;
-    double *lrec = nullptr, *psi_tmp = nullptr, *outq_tmp = nullptr, *outb_tmp = nullptr;
+    double *lrec = nullptr, *psi_tmp = nullptr, *outq_tmp = nullptr, *outb_tmp = nullptr, *tape = nullptr;
 
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     float last_res_ms = 0.f, last_vjp_ms = 0.f;

@@ -44,8 +44,9 @@ __device__ inline void bc_copy(T* g, const T* s) {
     g[P_T] = s[P_T]; g[P_NUT] = s[P_NUT];
 }
 
+// All threads of the block apply c.bcs[0..nbc) in order.
 template <class T, int NQ>
-__global__ void __launch_bounds__(1024) k_bc(DevCase c, T* __restrict__ P) {
+__device__ void bc_apply_block(const DevCase& c, T* __restrict__ P) {
     const int nic = c.nic, njc = c.njc;
     const double iR = 1.0 / c.R;
     for (int b = 0; b < c.nbc; b++) {
@@ -142,9 +143,14 @@ __global__ void __launch_bounds__(1024) k_bc(DevCase c, T* __restrict__ P) {
         }
         __syncthreads();
     }
-    // mu, mu_t of every ghost cell (eulerequation.cpp:183-188 covers the
-    // whole padded array)
-    if (c.viscous) {
+}
+
+// mu, mu_t of every ghost cell (eulerequation.cpp:183-188 covers the whole
+// padded array)
+template <class T, int NQ>
+__device__ void bc_ghost_mu(const DevCase& c, T* __restrict__ P) {
+    const int nic = c.nic, njc = c.njc;
+    {
         const int nring = 2 * (nic + 2) + 2 * njc;
         for (int r = threadIdx.x; r < nring; r += blockDim.x) {
             int ip, jp;
@@ -158,6 +164,12 @@ __global__ void __launch_bounds__(1024) k_bc(DevCase c, T* __restrict__ P) {
             g[P_MUT] = (NQ == 5 && val(mu) != 0.0) ? sa_mut(g[P_RHO], g[P_NUT], mu) : T(0.0);
         }
     }
+}
+
+template <class T, int NQ>
+__global__ void __launch_bounds__(1024) k_bc(DevCase c, T* __restrict__ P) {
+    bc_apply_block<T, NQ>(c, P);
+    if (c.viscous) bc_ghost_mu<T, NQ>(c, P);
 }
 
 // ----------------------------------------------------------------------------

@@ -70,6 +70,7 @@ def load_library() -> ctypes.CDLL:
         "st_probe_fp64": (I, [V, ctypes.POINTER(D)]),
         "st_last_kernel_ms": (I, [V, ctypes.POINTER(D), ctypes.POINTER(D)]),
         "st_profile_residual": (I, [V, I, _P, ctypes.POINTER(I)]),
+        "st_launch_counts": (I, [V, I, ctypes.POINTER(I), ctypes.POINTER(I)]),
         "st_device_state": (I, [V, ctypes.POINTER(V), ctypes.POINTER(V), ctypes.POINTER(V)]),
     }
     for name, (res, args) in sig.items():
@@ -203,6 +204,11 @@ class EulerEquation:
         n = ctypes.c_int()
         _check(self.lib.st_profile_residual(self.h, int(lhs), _ptr(ms), ctypes.byref(n)), "st_profile_residual")
         return ms[:n.value]
+
+    def launch_counts(self, lhs: bool = False):
+        r, v = ctypes.c_int(), ctypes.c_int()
+        _check(self.lib.st_launch_counts(self.h, int(lhs), ctypes.byref(r), ctypes.byref(v)), "st_launch_counts")
+        return r.value, v.value
 
     def last_kernel_ms(self):
         a, b = ctypes.c_double(), ctypes.c_double()
