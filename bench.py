@@ -139,25 +139,39 @@ def ensure_port():
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "port"], check=True)
 
 
-def cpu_baseline_sample(turbulence: str, budget_s: float, threads: int):
-    """Times the CPU restatement (oracle/port) of the residual on the
-    513x257 grid of the same workload for about budget_s seconds."""
+def time_port(port, q, psi, with_adj, budget_s=None, steps=None):
+    """Seconds per step of the CPU restatement: one residual, plus (with_adj)
+    one forward-mode dual-number pass (dR/dQ) v of the same Jacobian, the
+    operation-count class of a taped reverse sweep."""
+    port.residual(q)
+    if with_adj:
+        port.jvp(q, psi)
+    n, t0 = 0, time.perf_counter()
+    while True:
+        port.residual(q)
+        if with_adj:
+            port.jvp(q, psi)
+        n += 1
+        el = time.perf_counter() - t0
+        if (steps is not None and n >= steps) or (budget_s is not None and el > budget_s):
+            break
+    return el / n, n
+
+
+def cpu_baseline_sample(turbulence: str, budget_s: float, threads: int, with_adj: bool):
+    """Times the CPU restatement (oracle/port) on the 513x257 grid of the
+    same workload for about budget_s seconds."""
     ensure_port()
     from oracle.port import PortCase
     c, xv, yv, q = build_case("513x257", turbulence)
     port = PortCase(c, xv, yv)
     used = port.set_threads(threads)
-    port.residual(q)
-    n, t0 = 0, time.perf_counter()
-    while True:
-        port.residual(q)
-        n += 1
-        if time.perf_counter() - t0 > budget_s:
-            break
-    dt = (time.perf_counter() - t0) / n
+    psi = np.random.default_rng(SEED + 1).standard_normal(q.shape)
+    dt, n = time_port(port, q, psi, with_adj, budget_s=budget_s)
+    what = "residual + dual-number JVP (adjoint-class pass)" if with_adj else "residual"
     return {"value": c.nic * c.njc / dt / 1e6, "unit": "Mcells/s", "cores": used, "kind": "port",
-            "sample": "%d residual evaluations of the 513x257 grid of the same workload (%s), %.1f s"
-                      % (n, turbulence, n * dt)}
+            "sample": "%d steps (%s) of the 513x257 grid of the same workload (%s), %.1f s"
+                      % (n, what, turbulence, n * dt)}
 
 
 def run_reference(args, world, rank):
@@ -166,38 +180,39 @@ def run_reference(args, world, rank):
     threads = os.cpu_count() or 1
     ensure_port()
     from oracle.port import PortCase
-    # per step: one residual of a grid of this workload sized for the budget
+    with_adj = not args.residual_only
+    # per step: one residual (+ adjoint-class pass) of the largest grid of this
+    # workload that fits the time budget
     budget = 150.0 / max(1, args.steps + args.warmup)
     grid = "513x257"
     c, xv, yv, q = build_case(grid, args.turbulence)
     port = PortCase(c, xv, yv)
     port.set_threads(threads)
-    t0 = time.perf_counter()
-    port.residual(q)
-    t1 = time.perf_counter() - t0
+    psi = np.random.default_rng(SEED + 1).standard_normal(q.shape)
+    t1, _ = time_port(port, q, psi, with_adj, steps=1)
     for g in ("2049x1025", "4097x2049"):
         ni, nj = GRIDS[g]
-        est = t1 * (ni - 1) * (nj - 1) / (c.nic * c.njc)
-        if est < budget:
+        if t1 * (ni - 1) * (nj - 1) / (c.nic * c.njc) < budget:
             grid = g
     if grid != "513x257":
         c, xv, yv, q = build_case(grid, args.turbulence)
         port = PortCase(c, xv, yv)
         port.set_threads(threads)
+        psi = np.random.default_rng(SEED + 1).standard_normal(q.shape)
     for _ in range(args.warmup):
         port.residual(q)
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        port.residual(q)
-    el = time.perf_counter() - t0
+        if with_adj:
+            port.jvp(q, psi)
+    dt, _ = time_port(port, q, psi, with_adj, steps=args.steps)
     cells = c.nic * c.njc
-    v = cells * args.steps / el / 1e6
-    line = {"impl": "reference", "metric": metric_name(False), "value": v, "unit": "Mcells/s",
-            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
+    v = cells / dt / 1e6
+    what = "residual + dual-number JVP pass" if with_adj else "residual"
+    line = {"impl": "reference", "metric": metric_name(with_adj), "value": v, "unit": "Mcells/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": workload_config(args, grid),
+            "data": "synthetic", "config": workload_config(args, args.grid),
             "cpu_baseline": {"value": v, "unit": "Mcells/s", "cores": threads, "kind": "port",
-                             "sample": "residual of the %s grid of the workload per step, %d steps" % (grid, args.steps)},
+                             "sample": "%s of the %s grid of the workload per step, %d steps" % (what, grid, args.steps)},
             "e2e": {"value": v, "unit": "Mcells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -233,7 +248,7 @@ def run_ours(args, world, rank, local):
     psi = torch.tensor(rng.standard_normal(q.shape), device="cuda")
     outq = torch.empty_like(psi)
     outb = torch.empty((c.nic, c.njc), dtype=torch.float64, device="cuda")
-    with_adj = True
+    with_adj = not args.residual_only
     try:
         eq.vjp_device(psi.data_ptr(), outq.data_ptr(), outb.data_ptr())
         torch.cuda.synchronize()
@@ -347,7 +362,7 @@ def run_ours(args, world, rank, local):
             "config": workload_config(args, args.grid), "roofline": roof, "e2e": e2e,
             "clocks": clk.summary(), "gpu_launches": kernels_per_step * args.steps}
     if world == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline_sample(tb, 12.0, os.cpu_count() or 1)
+        line["cpu_baseline"] = cpu_baseline_sample(tb, 12.0, os.cpu_count() or 1, with_adj)
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -362,6 +377,7 @@ def main():
     ap.add_argument("--grid", choices=sorted(GRIDS), default="4097x2049")
     ap.add_argument("--turbulence", choices=["sa", "none"], default="sa")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--residual-only", action="store_true", help="time the residual without the adjoint")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -737,7 +737,9 @@ void residual(const PCase& pc, const T* q, const T* beta, T* rhs, int order, Wor
 struct Handle {
     PCase pc;
     Work<double> wd;
-    std::vector<Work<Dual>> wdual;  // one per OpenMP thread
+    Work<Dual> wjvp;                 // reused by port_jvp
+    std::vector<Dual> qd, bd, rd;
+    bool jvp_ready = false;
 };
 
 }  // namespace
@@ -840,13 +842,21 @@ int port_jvp(void* hp, const double* q, const double* beta, const double* v, con
     auto* h = static_cast<Handle*>(hp);
     const PCase& pc = h->pc;
     const size_t n = (size_t)pc.nic * pc.njc * pc.nq, nc = (size_t)pc.nic * pc.njc;
-    std::vector<Dual> qd(n), bd(nc), rd(n);
-    for (size_t i = 0; i < n; i++) qd[i] = Dual(q[i], v[i]);
-    for (size_t i = 0; i < nc; i++) bd[i] = Dual(beta ? beta[i] : 1.0, vb ? vb[i] : 0.0);
-    Work<Dual> w;
-    w.init(pc);
-    residual<Dual>(pc, qd.data(), bd.data(), rd.data(), order, w);
-    for (size_t i = 0; i < n; i++) jv[i] = rd[i].d;
+    if (!h->jvp_ready) {
+        h->qd.resize(n); h->bd.resize(nc); h->rd.resize(n);
+        h->wjvp.init(pc);
+        h->jvp_ready = true;
+    }
+    std::vector<Dual>& qd = h->qd;
+    std::vector<Dual>& bd = h->bd;
+    std::vector<Dual>& rd = h->rd;
+#pragma omp parallel for schedule(static)
+    for (long i = 0; i < (long)n; i++) qd[i] = Dual(q[i], v[i]);
+#pragma omp parallel for schedule(static)
+    for (long i = 0; i < (long)nc; i++) bd[i] = Dual(beta ? beta[i] : 1.0, vb ? vb[i] : 0.0);
+    residual<Dual>(pc, qd.data(), bd.data(), rd.data(), order, h->wjvp);
+#pragma omp parallel for schedule(static)
+    for (long i = 0; i < (long)n; i++) jv[i] = rd[i].d;
     return 0;
 }
 
