@@ -285,13 +285,10 @@ def run_ours(args, world, rank, local):
     value = world * cells * args.steps / (el_ms * 1e-3) / 1e6
 
     # per-launch attribution (outside the timed region)
-    kern_ms = eq.profile_residual()
-    res_ms = float(np.sum(kern_ms))
-    adj_ms = 0.0
-    if with_adj:
-        for _ in range(3):
-            eq.vjp_device(psi.data_ptr(), outq.data_ptr(), outb.data_ptr())
-        adj_ms = eq.last_kernel_ms()[1]
+    kern_res = eq.profile("residual")
+    res_ms = float(sum(kern_res.values()))
+    kern_adj = eq.profile("adjoint") if with_adj else {}
+    adj_ms = float(sum(kern_adj.values()))
     fp64_peak = eq.probe_fp64_tflops()
 
     # end to end through the host-buffer C ABI: pinned q in, rhs (+ adjoint) out
@@ -348,8 +345,7 @@ def run_ours(args, world, rank, local):
             "traffic": traffic_cell * cells if traffic_cell else None,
             "scope": "whole residual%s evaluation (%d launches), %d algorithmic B/cell"
                      % ("+adjoint" if with_adj else "", kernels_per_step, alg),
-            "kernels_ms": {"prim": kern_ms[0], "bc": kern_ms[1], "limiter": kern_ms[2], "face_i": kern_ms[3],
-                           "face_j": kern_ms[4], "cell": kern_ms[5], "adjoint_total": adj_ms}}
+            "kernels_ms": {"residual": kern_res, "adjoint": kern_adj}}
     if flops_cell:
         fp64_ach = flops_cell * cells / (res_ms * 1e-3) / 1e12
         roof["fp64"] = {"achieved_tflops": fp64_ach, "peak_tflops": fp64_peak, "frac": fp64_ach / fp64_peak,

@@ -134,11 +134,12 @@ int st_launch_counts(st_ctx* ctx, int lhs, int* residual, int* vjp);
 
 /* Diagnostics: dense FP64 FMA throughput of this device (TFLOP/s). */
 int st_probe_fp64(st_ctx* ctx, double* tflops);
-/* Runs the residual pipeline once on the context state with a CUDA event
- * between launches: ms[k] is the device time of launch k, *nkernels the count
- * (at most 8).  Order: primitives, boundary conditions, limiter, i-faces,
- * j-faces, cell assembly. */
-int st_profile_residual(st_ctx* ctx, int lhs, double* ms, int* nkernels);
+/* Runs one pipeline on the context state (which = 0: residual; 1: adjoint VJP
+ * with psi = the context's last residual) with a CUDA event after every
+ * launch: ms[k] is the device time of launch k, names a comma-separated list
+ * of kernel names, *n the launch count (at most max_n). */
+int st_profile_pipeline(st_ctx* ctx, int which, int lhs, double* ms, int max_n, char* names, int names_len,
+                        int* n);
 /* Device time (ms) of the last residual / VJP launch sequence, CUDA events on
  * the context stream (waits for them).  The *_device entry points are
  * asynchronous on the context stream; the host-buffer ones synchronise. */

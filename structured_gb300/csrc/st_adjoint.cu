@@ -44,20 +44,34 @@ int launch_vjp(st_ctx* x, const double* psi, double* outq, double* outb) {
     const DevCase& dc = x->dc;
     const unsigned gc = grid_for(x->ncell);
     k_prim<double, NQ><<<gc, 256, 0, s>>>(dc, x->q, x->P);
+    stx::mark(x, "k_prim");
     k_bc_taped<NQ><<<1, 1024, 0, s>>>(dc, x->P, x->tape);
-    if (ORDER == 2) k_limiter<double, NQ><<<gc, 256, 0, s>>>(dc, x->P, x->phi_i, x->phi_j);
+    stx::mark(x, "k_bc_taped");
+    if (ORDER == 2) {
+        k_limiter<double, NQ><<<gc, 256, 0, s>>>(dc, x->P, x->phi_i, x->phi_j);
+        stx::mark(x, "k_limiter");
+    }
     if (NQ == 5 && dc.viscous) {
         k_face_grad<0><<<grid_for(x->nfi), 256, 0, s>>>(dc, x->P, x->Gi);
         k_face_grad<1><<<grid_for(x->nfj), 256, 0, s>>>(dc, x->P, x->Gj);
+        stx::mark(x, "k_face_grad(i+j)");
     }
     k_cell_adj<NQ><<<gc, 256, 0, s>>>(dc, x->P, x->Gi, x->Gj, x->beta, psi, x->w, x->srec, outb);
+    stx::mark(x, "k_cell_adj");
     k_face_adj<NQ, 0, ORDER><<<grid_for(x->nfi), 256, 0, s>>>(dc, x->P, x->phi_i, x->w, x->srec, x->arec_i);
+    stx::mark(x, "k_face_adj_i");
     k_face_adj<NQ, 1, ORDER><<<grid_for(x->nfj), 256, 0, s>>>(dc, x->P, x->phi_j, x->w, x->srec, x->arec_j);
-    if (ORDER == 2)
+    stx::mark(x, "k_face_adj_j");
+    if (ORDER == 2) {
         k_limiter_adj<NQ><<<gc, 256, 0, s>>>(dc, x->P, x->phi_i, x->phi_j, x->arec_i, x->arec_j, x->lrec);
+        stx::mark(x, "k_limiter_adj");
+    }
     k_gather<NQ, ORDER><<<grid_for(x->npad), 256, 0, s>>>(dc, x->P, x->arec_i, x->arec_j, x->lrec, x->srec, x->Pbar);
+    stx::mark(x, "k_gather");
     k_bc_adj<NQ><<<1, 1024, 0, s>>>(dc, x->P, x->tape, x->Pbar);
+    stx::mark(x, "k_bc_adj");
     k_prim_adj<NQ><<<gc, 256, 0, s>>>(dc, x->q, x->P, x->Pbar, outq);
+    stx::mark(x, "k_prim_adj");
     ST_LAUNCH_CHECK("vjp launch");
     return ST_OK;
 }

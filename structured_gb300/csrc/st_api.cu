@@ -288,16 +288,24 @@ int launch_forward(st_ctx* x, const DevCase& dc, const T* q, const T* beta, T* P
     cudaStream_t s = x->stream;
     const unsigned gc = grid_for(x->ncell);
     k_prim<T, NQ><<<gc, 256, 0, s>>>(dc, q, P);
+    stx::mark(x, "k_prim");
     k_bc<T, NQ><<<1, 1024, 0, s>>>(dc, P);
+    stx::mark(x, "k_bc");
     if (order == 2) {
         k_limiter<T, NQ><<<gc, 256, 0, s>>>(dc, P, phi_i, phi_j);
+        stx::mark(x, "k_limiter");
         k_face<T, NQ, 0, 2><<<grid_for(x->nfi), 256, 0, s>>>(dc, P, phi_i, Fi, Gi);
+        stx::mark(x, "k_face_i");
         k_face<T, NQ, 1, 2><<<grid_for(x->nfj), 256, 0, s>>>(dc, P, phi_j, Fj, Gj);
+        stx::mark(x, "k_face_j");
     } else {
         k_face<T, NQ, 0, 1><<<grid_for(x->nfi), 256, 0, s>>>(dc, P, phi_i, Fi, Gi);
+        stx::mark(x, "k_face_i");
         k_face<T, NQ, 1, 1><<<grid_for(x->nfj), 256, 0, s>>>(dc, P, phi_j, Fj, Gj);
+        stx::mark(x, "k_face_j");
     }
     k_cell<T, NQ><<<gc, 256, 0, s>>>(dc, P, Fi, Fj, Gi, Gj, beta, rhs);
+    stx::mark(x, "k_cell");
     ST_LAUNCH_CHECK("residual launch");
     return ST_OK;
 }
@@ -639,45 +647,37 @@ int st_probe_fp64(st_ctx* x, double* tflops) {
     return ST_OK;
 }
 
-// Runs the residual pipeline once on the context state with an event
-// between kernels; ms[k] = device time of launch k (at most 8 entries).
-int st_profile_residual(st_ctx* x, int lhs, double* ms, int* nkernels) {
-    if (!x || !ms || !nkernels) return fail(ST_ERR_ARG, "st_profile_residual: null argument");
-    cudaEvent_t ev[8];
-    for (auto& e : ev) cudaEventCreate(&e);
-    cudaStream_t s = x->stream;
-    const DevCase& dc = x->dc;
-    const int order = order_of(x, lhs);
-    const unsigned gc = grid_for(x->ncell);
-    int n = 0;
-    cudaEventRecord(ev[n++], s);
-#define PROF_PIPE(NQ)                                                                                  \
-    k_prim<double, NQ><<<gc, 256, 0, s>>>(dc, x->q, x->P); cudaEventRecord(ev[n++], s);                \
-    k_bc<double, NQ><<<1, 1024, 0, s>>>(dc, x->P); cudaEventRecord(ev[n++], s);                         \
-    k_limiter<double, NQ><<<gc, 256, 0, s>>>(dc, x->P, x->phi_i, x->phi_j); cudaEventRecord(ev[n++], s); \
-    if (order == 2) {                                                                                  \
-        k_face<double, NQ, 0, 2><<<grid_for(x->nfi), 256, 0, s>>>(dc, x->P, x->phi_i, x->Fi, x->Gi);     \
-        cudaEventRecord(ev[n++], s);                                                                   \
-        k_face<double, NQ, 1, 2><<<grid_for(x->nfj), 256, 0, s>>>(dc, x->P, x->phi_j, x->Fj, x->Gj);     \
-    } else {                                                                                           \
-        k_face<double, NQ, 0, 1><<<grid_for(x->nfi), 256, 0, s>>>(dc, x->P, x->phi_i, x->Fi, x->Gi);     \
-        cudaEventRecord(ev[n++], s);                                                                   \
-        k_face<double, NQ, 1, 1><<<grid_for(x->nfj), 256, 0, s>>>(dc, x->P, x->phi_j, x->Fj, x->Gj);     \
-    }                                                                                                  \
-    cudaEventRecord(ev[n++], s);                                                                       \
-    k_cell<double, NQ><<<gc, 256, 0, s>>>(dc, x->P, x->Fi, x->Fj, x->Gi, x->Gj, x->beta, x->rhs);        \
-    cudaEventRecord(ev[n++], s);
-    if (x->nq == 5) { PROF_PIPE(5) } else { PROF_PIPE(4) }
-#undef PROF_PIPE
-    cudaError_t e = cudaEventSynchronize(ev[n - 1]);
-    for (int k = 0; k + 1 < n; k++) {
+// Runs one pipeline (which = 0 residual, 1 adjoint VJP with psi = the
+// context's last residual) with a CUDA event after every launch and returns
+// the per-launch device times and names.
+int st_profile_pipeline(st_ctx* x, int which, int lhs, double* ms, int max_n, char* names, int names_len,
+                        int* n) {
+    if (!x || !ms || !n) return fail(ST_ERR_ARG, "st_profile_pipeline: null argument");
+    if (!x->prof_ev[0])
+        for (auto& e : x->prof_ev) cudaEventCreate(&e);
+    x->prof_on = true;
+    x->prof_n = 0;
+    cudaEventRecord(x->prof_ev[0], x->stream);
+    int rc;
+    if (which == 0) rc = stx::run_residual(x, x->q, x->beta, x->rhs, order_of(x, lhs));
+    else rc = st_vjp_device(x, x->rhs, nullptr, nullptr, lhs);
+    x->prof_on = false;
+    if (rc) return rc;
+    ST_CUDA(cudaEventSynchronize(x->prof_ev[x->prof_n]));
+    const int cnt = std::min(x->prof_n, max_n);
+    std::string all;
+    for (int k = 0; k < cnt; k++) {
         float t = 0.f;
-        cudaEventElapsedTime(&t, ev[k], ev[k + 1]);
+        cudaEventElapsedTime(&t, x->prof_ev[k], x->prof_ev[k + 1]);
         ms[k] = t;
+        if (k) all += ",";
+        all += x->prof_name[k + 1];
     }
-    *nkernels = n - 1;
-    for (auto& ee : ev) cudaEventDestroy(ee);
-    if (e != cudaSuccess) return stx::cuda_fail(e, "st_profile_residual");
+    if (names && names_len > 0) {
+        std::strncpy(names, all.c_str(), names_len - 1);
+        names[names_len - 1] = 0;
+    }
+    *n = cnt;
     return ST_OK;
 }
 

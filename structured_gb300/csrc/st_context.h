@@ -38,6 +38,11 @@ struct st_ctx {
     double *lrec = nullptr, *psi_tmp = nullptr, *outq_tmp = nullptr, *outb_tmp = nullptr, *tape = nullptr;
 
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    // per-launch profiling (st_profile_pipeline): an event after each launch
+    bool prof_on = false;
+    int prof_n = 0;
+    cudaEvent_t prof_ev[33] = {};
+    const char* prof_name[33] = {};
     float last_res_ms = 0.f, last_vjp_ms = 0.f;
     bool have_residual = false;
     bool res_pending = false, vjp_pending = false;
@@ -61,6 +66,13 @@ inline unsigned grid_for(size_t n, unsigned threads = 256) {
     if (g < 1) g = 1;
     if (g > (1u << 30)) g = 1u << 30;
     return (unsigned)g;
+}
+// records a profiling event after a launch when profiling is on
+inline void mark(st_ctx* x, const char* name) {
+    if (!x->prof_on || x->prof_n >= 32) return;
+    cudaEventRecord(x->prof_ev[x->prof_n + 1], x->stream);
+    x->prof_name[x->prof_n + 1] = name;
+    x->prof_n++;
 }
 // forward pipeline on (q -> rhs) for the double path; beta may be null
 int run_residual(st_ctx* ctx, const double* q, const double* beta, double* rhs, int order);

@@ -69,7 +69,7 @@ def load_library() -> ctypes.CDLL:
         "st_vjp": (I, [V, _P, _P, _P, I]),
         "st_probe_fp64": (I, [V, ctypes.POINTER(D)]),
         "st_last_kernel_ms": (I, [V, ctypes.POINTER(D), ctypes.POINTER(D)]),
-        "st_profile_residual": (I, [V, I, _P, ctypes.POINTER(I)]),
+        "st_profile_pipeline": (I, [V, I, I, _P, I, ctypes.c_char_p, I, ctypes.POINTER(I)]),
         "st_launch_counts": (I, [V, I, ctypes.POINTER(I), ctypes.POINTER(I)]),
         "st_device_state": (I, [V, ctypes.POINTER(V), ctypes.POINTER(V), ctypes.POINTER(V)]),
     }
@@ -199,11 +199,18 @@ class EulerEquation:
         _check(self.lib.st_probe_fp64(self.h, ctypes.byref(t)), "st_probe_fp64")
         return t.value
 
-    def profile_residual(self, lhs: bool = False):
-        ms = np.zeros(8)
+    def profile(self, which: str = "residual", lhs: bool = False) -> dict:
+        """Per-launch device times (ms) of one residual or adjoint evaluation."""
+        ms = np.zeros(32)
+        buf = ctypes.create_string_buffer(1024)
         n = ctypes.c_int()
-        _check(self.lib.st_profile_residual(self.h, int(lhs), _ptr(ms), ctypes.byref(n)), "st_profile_residual")
-        return ms[:n.value]
+        _check(self.lib.st_profile_pipeline(self.h, 0 if which == "residual" else 1, int(lhs), _ptr(ms), 32, buf,
+                                            1024, ctypes.byref(n)), "st_profile_pipeline")
+        names = buf.value.decode().split(",")
+        out = {}
+        for k, v in zip(names, ms[:n.value]):
+            out[k] = out.get(k, 0.0) + float(v)
+        return out
 
     def launch_counts(self, lhs: bool = False):
         r, v = ctypes.c_int(), ctypes.c_int()
