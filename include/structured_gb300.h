@@ -128,6 +128,17 @@ int st_jvp_device(st_ctx* ctx, const double* v_dev, const double* vb_dev, double
 int st_vjp_device(st_ctx* ctx, const double* psi_dev, double* out_q_dev, double* out_beta_dev, int lhs);
 /* Host-buffer variant (copies in the timed path). */
 int st_vjp(st_ctx* ctx, const double* psi_host, double* out_q_host, double* out_beta_host, int lhs);
+/* Residual and adjoint of the same state in one sweep (the forward passes
+ * are shared and each face pass computes its flux and its reverse at once):
+ * rhs as st_residual_device, products as st_vjp_device.  psi must not alias
+ * rhs.  Device pointers; outputs may be NULL except rhs. */
+int st_residual_vjp_device(st_ctx* ctx, const double* psi_dev, double* rhs_dev, double* out_q_dev,
+                           double* out_beta_dev, int lhs);
+/* Host-buffer variant of st_residual_vjp_device (on the context state). */
+int st_residual_vjp(st_ctx* ctx, const double* psi_host, double* rhs_host, double* out_q_host,
+                    double* out_beta_host, int lhs);
+/* Kernel launches one st_residual_vjp_device call makes. */
+int st_fused_launch_count(st_ctx* ctx, int lhs);
 
 /* Kernel launches one st_residual_device / st_vjp_device call makes. */
 int st_launch_counts(st_ctx* ctx, int lhs, int* residual, int* vjp);
@@ -135,7 +146,7 @@ int st_launch_counts(st_ctx* ctx, int lhs, int* residual, int* vjp);
 /* Diagnostics: dense FP64 FMA throughput of this device (TFLOP/s). */
 int st_probe_fp64(st_ctx* ctx, double* tflops);
 /* Runs one pipeline on the context state (which = 0: residual; 1: adjoint VJP
- * with psi = the context's last residual) with a CUDA event after every
+ * with psi = the context's last residual; 2: residual + VJP in one sweep) with a CUDA event after every
  * launch: ms[k] is the device time of launch k, names a comma-separated list
  * of kernel names, *n the launch count (at most max_n). */
 int st_profile_pipeline(st_ctx* ctx, int which, int lhs, double* ms, int max_n, char* names, int names_len,

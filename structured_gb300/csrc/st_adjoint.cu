@@ -24,11 +24,9 @@ int ensure(st_ctx* x) {
     const size_t ring = 2 * (size_t)(x->c.ni + 1) + 2 * (size_t)(x->c.nj - 1);
     int rc = ST_OK;
     if (rc == ST_OK) rc = alloc_d(&x->Pbar, x->npad * NP);
-    if (rc == ST_OK) rc = alloc_d(&x->w, x->ncell * nq);
     if (rc == ST_OK) rc = alloc_d(&x->srec, x->ncell * SRW);
     if (rc == ST_OK) rc = alloc_d(&x->arec_i, x->nfi * ARW);
     if (rc == ST_OK) rc = alloc_d(&x->arec_j, x->nfj * ARW);
-    if (rc == ST_OK) rc = alloc_d(&x->lrec, x->ncell * 4 * nq);
     if (rc == ST_OK) rc = alloc_d(&x->tape, std::max(1, x->c.nbc) * ring * RW);
     if (rc == ST_OK) rc = alloc_d(&x->psi_tmp, x->ncell * nq);
     if (rc == ST_OK) rc = alloc_d(&x->outq_tmp, x->ncell * nq);
@@ -38,8 +36,10 @@ int ensure(st_ctx* x) {
     return ST_OK;
 }
 
+// Residual (when rhs != null) and adjoint in one sweep: the forward passes are
+// shared, and each face pass computes its flux and runs its reverse at once.
 template <int NQ, int ORDER>
-int launch_vjp(st_ctx* x, const double* psi, double* outq, double* outb) {
+int launch_fused(st_ctx* x, const double* psi, double* rhs, double* outq, double* outb) {
     cudaStream_t s = x->stream;
     const DevCase& dc = x->dc;
     const unsigned gc = grid_for(x->ncell);
@@ -48,39 +48,52 @@ int launch_vjp(st_ctx* x, const double* psi, double* outq, double* outb) {
     k_bc_taped<NQ><<<1, 1024, 0, s>>>(dc, x->P, x->tape);
     stx::mark(x, "k_bc_taped");
     if (ORDER == 2) {
-        k_limiter<double, NQ><<<gc, 256, 0, s>>>(dc, x->P, x->phi_i, x->phi_j);
-        stx::mark(x, "k_limiter");
+        k_limiter<double, NQ, true><<<gc, 256, 0, s>>>(dc, x->P, x->lim);
+        stx::mark(x, "k_limiter_adj");
     }
     if (NQ == 5 && dc.viscous) {
         k_face_grad<0><<<grid_for(x->nfi), 256, 0, s>>>(dc, x->P, x->Gi);
         k_face_grad<1><<<grid_for(x->nfj), 256, 0, s>>>(dc, x->P, x->Gj);
         stx::mark(x, "k_face_grad(i+j)");
+        k_cell_src<<<gc, 256, 0, s>>>(dc, x->P, x->Gi, x->Gj, x->beta, psi, x->srec, outb);
+        stx::mark(x, "k_cell_src");
     }
-    k_cell_adj<NQ><<<gc, 256, 0, s>>>(dc, x->P, x->Gi, x->Gj, x->beta, psi, x->w, x->srec, outb);
-    stx::mark(x, "k_cell_adj");
-    k_face_adj<NQ, 0, ORDER><<<grid_for(x->nfi), 256, 0, s>>>(dc, x->P, x->phi_i, x->w, x->srec, x->arec_i);
-    stx::mark(x, "k_face_adj_i");
-    k_face_adj<NQ, 1, ORDER><<<grid_for(x->nfj), 256, 0, s>>>(dc, x->P, x->phi_j, x->w, x->srec, x->arec_j);
-    stx::mark(x, "k_face_adj_j");
-    if (ORDER == 2) {
-        k_limiter_adj<NQ><<<gc, 256, 0, s>>>(dc, x->P, x->phi_i, x->phi_j, x->arec_i, x->arec_j, x->lrec);
-        stx::mark(x, "k_limiter_adj");
+    k_face_fused<NQ, 0, ORDER><<<grid_for(x->nfi), 256, 0, s>>>(dc, x->P, x->lim, psi, x->srec, rhs ? x->Fi : nullptr,
+                                                                x->arec_i);
+    stx::mark(x, "k_face_fused_i");
+    k_face_fused<NQ, 1, ORDER><<<grid_for(x->nfj), 256, 0, s>>>(dc, x->P, x->lim, psi, x->srec, rhs ? x->Fj : nullptr,
+                                                                x->arec_j);
+    stx::mark(x, "k_face_fused_j");
+    if (rhs) {
+        k_cell_res<NQ><<<gc, 256, 0, s>>>(dc, x->Fi, x->Fj, x->srec, rhs);
+        stx::mark(x, "k_cell_res");
     }
-    k_gather<NQ, ORDER><<<grid_for(x->npad), 256, 0, s>>>(dc, x->P, x->arec_i, x->arec_j, x->lrec, x->srec, x->Pbar);
+    k_gather<NQ, ORDER><<<grid_for(x->npad), 256, 0, s>>>(dc, x->P, x->arec_i, x->arec_j, x->srec, x->Pbar);
     stx::mark(x, "k_gather");
     k_bc_adj<NQ><<<1, 1024, 0, s>>>(dc, x->P, x->tape, x->Pbar);
     stx::mark(x, "k_bc_adj");
     k_prim_adj<NQ><<<gc, 256, 0, s>>>(dc, x->q, x->P, x->Pbar, outq);
     stx::mark(x, "k_prim_adj");
-    ST_LAUNCH_CHECK("vjp launch");
+    ST_LAUNCH_CHECK("residual/adjoint launch");
     return ST_OK;
 }
 
-int vjp_launches(const st_ctx* x, int order) {
-    int n = 8;  // prim, bc, cell_adj, face_adj x2, gather, bc_adj, prim_adj
-    if (order == 2) n += 2;  // limiter, limiter_adj
-    if (x->nq == 5 && x->dc.viscous) n += 2;  // face gradient parts
+int fused_launches(const st_ctx* x, int order, bool with_rhs) {
+    int n = 7;  // prim, bc, face x2, gather, bc_adj, prim_adj
+    if (order == 2) n += 1;
+    if (x->nq == 5 && x->dc.viscous) n += 3;
+    if (with_rhs) n += 1;
     return n;
+}
+
+int run_fused(st_ctx* x, const double* psi, double* rhs, double* outq, double* outb, int lhs) {
+    int rc = ensure(x);
+    if (rc) return rc;
+    const int order = lhs ? x->c.lhs_order : x->c.order;
+    if (x->nq == 4 || !x->dc.viscous) ST_CUDA(cudaMemsetAsync(outb, 0, x->ncell * 8, x->stream));
+    if (x->nq == 5) rc = order == 2 ? launch_fused<5, 2>(x, psi, rhs, outq, outb) : launch_fused<5, 1>(x, psi, rhs, outq, outb);
+    else rc = order == 2 ? launch_fused<4, 2>(x, psi, rhs, outq, outb) : launch_fused<4, 1>(x, psi, rhs, outq, outb);
+    return rc;
 }
 
 }  // namespace
@@ -91,13 +104,20 @@ int st_vjp_device(st_ctx* x, const double* psi, double* outq, double* outb, int 
     if (!x || !psi) return fail(ST_ERR_ARG, "st_vjp_device: null argument");
     int rc = ensure(x);
     if (rc) return rc;
-    const int order = lhs ? x->c.lhs_order : x->c.order;
-    double* oq = outq ? outq : x->outq_tmp;
-    double* ob = outb ? outb : x->outb_tmp;
-    if (x->nq == 4) ST_CUDA(cudaMemsetAsync(ob, 0, x->ncell * 8, x->stream));
     cudaEventRecord(x->ev[2], x->stream);
-    if (x->nq == 5) rc = order == 2 ? launch_vjp<5, 2>(x, psi, oq, ob) : launch_vjp<5, 1>(x, psi, oq, ob);
-    else rc = order == 2 ? launch_vjp<4, 2>(x, psi, oq, ob) : launch_vjp<4, 1>(x, psi, oq, ob);
+    rc = run_fused(x, psi, nullptr, outq ? outq : x->outq_tmp, outb ? outb : x->outb_tmp, lhs);
+    if (rc) return rc;
+    cudaEventRecord(x->ev[3], x->stream);
+    x->vjp_pending = true;
+    return ST_OK;
+}
+
+int st_residual_vjp_device(st_ctx* x, const double* psi, double* rhs, double* outq, double* outb, int lhs) {
+    if (!x || !psi || !rhs) return fail(ST_ERR_ARG, "st_residual_vjp_device: null argument");
+    int rc = ensure(x);
+    if (rc) return rc;
+    cudaEventRecord(x->ev[2], x->stream);
+    rc = run_fused(x, psi, rhs, outq ? outq : x->outq_tmp, outb ? outb : x->outb_tmp, lhs);
     if (rc) return rc;
     cudaEventRecord(x->ev[3], x->stream);
     x->vjp_pending = true;
@@ -117,12 +137,32 @@ int st_vjp(st_ctx* x, const double* psi_host, double* outq_host, double* outb_ho
     return ST_OK;
 }
 
+int st_residual_vjp(st_ctx* x, const double* psi_host, double* rhs_host, double* outq_host, double* outb_host, int lhs) {
+    if (!x || !psi_host) return fail(ST_ERR_ARG, "st_residual_vjp: null argument");
+    int rc = ensure(x);
+    if (rc) return rc;
+    ST_CUDA(cudaMemcpyAsync(x->psi_tmp, psi_host, x->ncell * x->nq * 8, cudaMemcpyHostToDevice, x->stream));
+    rc = st_residual_vjp_device(x, x->psi_tmp, x->rhs, x->outq_tmp, x->outb_tmp, lhs);
+    if (rc) return rc;
+    x->have_residual = true;
+    if (rhs_host) ST_CUDA(cudaMemcpyAsync(rhs_host, x->rhs, x->ncell * x->nq * 8, cudaMemcpyDeviceToHost, x->stream));
+    if (outq_host) ST_CUDA(cudaMemcpyAsync(outq_host, x->outq_tmp, x->ncell * x->nq * 8, cudaMemcpyDeviceToHost, x->stream));
+    if (outb_host) ST_CUDA(cudaMemcpyAsync(outb_host, x->outb_tmp, x->ncell * 8, cudaMemcpyDeviceToHost, x->stream));
+    ST_CUDA(cudaStreamSynchronize(x->stream));
+    return ST_OK;
+}
+
 int st_launch_counts(st_ctx* x, int lhs, int* residual, int* vjp) {
     if (!x) return fail(ST_ERR_ARG, "st_launch_counts: null context");
     const int order = lhs ? x->c.lhs_order : x->c.order;
     if (residual) *residual = order == 2 ? 6 : 5;
-    if (vjp) *vjp = vjp_launches(x, order);
+    if (vjp) *vjp = fused_launches(x, order, false);
     return ST_OK;
+}
+
+int st_fused_launch_count(st_ctx* x, int lhs) {
+    if (!x) return fail(ST_ERR_ARG, "st_fused_launch_count: null context");
+    return fused_launches(x, lhs ? x->c.lhs_order : x->c.order, true);
 }
 
 }  // extern "C"

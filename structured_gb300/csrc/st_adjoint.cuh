@@ -14,157 +14,180 @@
 
 namespace st {
 
-// face adjoint record layout (ARW doubles per face)
+// Face adjoint record (ARW doubles per face).  The low cell L and high cell R
+// of the face each get three parts per reconstructed primitive k (rho,u,v,p,
+// nut): the adjoint of its reconstructed state (direct term) and the
+// adjoint's contribution to the cell's d- and d+ through its slope
+// (k_limiter<ADJ> stores the slope derivatives).  Then the adjoints of the
+// face gradients and face averages of the viscous flux.
 enum {
-    A_QL = 0,          // [5] adjoint of the left reconstructed state (rho,u,v,p,nut)
-    A_QR = 5,          // [5] right state
-    A_DUDX = 10, A_DUDY, A_DVDX, A_DVDY, A_DTDX, A_DTDY,
+    A_AL = 0, A_DML = 5, A_DPL = 10,    // L: direct, d-, d+
+    A_BR = 15, A_DMR = 20, A_DPR = 25,  // R: direct, d-, d+
+    A_DUDX = 30, A_DUDY, A_DVDX, A_DVDY, A_DTDX, A_DTDY,
     A_UB, A_VB, A_MUB, A_MUTB, A_DNDX, A_DNDY, A_RNB,
-    ARW = 24
+    ARW = 44
 };
-// per-cell source adjoint record: gbar (4), rho, nut, mu
-enum { S_GU = 0, S_GV, S_GNX, S_GNY, S_RHO, S_NUT, S_MU, SRW = 8 };
+// per-cell SA source record: gradient-part adjoints (4), rho, nut, mu
+// adjoints, and the source value itself
+enum { S_GU = 0, S_GV, S_GNX, S_GNY, S_RHO, S_NUT, S_MU, S_VAL, SRW = 8 };
 
 __device__ inline double sgn(double x) { return x < 0.0 ? -1.0 : 1.0; }
 
-// Reverse of roe_flux: given fb[0..3] (adjoint of f), accumulate the adjoints
-// of the eight face states.
-__device__ inline void roe_flux_adj(double rlft, double ulft, double vlft, double plft, double rrht, double urht,
-                                    double vrht, double prht, double r1, double r2, double aj, const double* fb,
-                                    double* bl, double* br) {
-    // ---- forward recompute -------------------------------------------------
-    const double rlfti = 1.0 / rlft;
-    const double rulft = rlft * ulft, rvlft = rlft * vlft;
-    const double uvl = 0.5 * (ulft * ulft + vlft * vlft);
-    const double elft = plft * OGM1 + rlft * uvl;
-    const double hlft = (elft + plft) * rlfti;
-    const double rrhti = 1.0 / rrht;
-    const double rurht = rrht * urht, rvrht = rrht * vrht;
-    const double uvr = 0.5 * (urht * urht + vrht * vrht);
-    const double erht = prht * OGM1 + rrht * uvr;
-    const double hrht = (erht + prht) * rrhti;
-    const double rat = ::sqrt(rrht * rlfti);
-    const double rati = 1.0 / (rat + 1.0);
-    const double rav = rat * rlft;
-    const double uav = (rat * urht + ulft) * rati;
-    const double vav = (rat * vrht + vlft) * rati;
-    const double hav = (rat * hrht + hlft) * rati;
-    const double uv = 0.5 * (uav * uav + vav * vav);
-    const double cav = ::sqrt(GM1 * (hav - uv));
-    const double aq1 = rrht - rlft, aq2 = urht - ulft, aq3 = vrht - vlft, aq4 = prht - plft;
-    const double uu = r1 * uav + r2 * vav;
-    const double c2 = cav * cav;
-    const double c2i = 1.0 / c2;
-    const double auu = ::fabs(uu), aupc = ::fabs(uu + cav), aumc = ::fabs(uu - cav);
-    const double uulft = r1 * ulft + r2 * vlft, uurht = r1 * urht + r2 * vrht;
-    const double rcav = rav * cav;
-    const double aquu = uurht - uulft;
-    const double c2ih = 0.5 * c2i;
-    const double ruuav = auu * rav;
-    const double t2 = aq4 + rcav * aquu, t3 = aq4 - rcav * aquu;
-    const double b1 = auu * (aq1 - c2i * aq4);
-    const double b2 = c2ih * aupc * t2;
-    const double b3 = c2ih * aumc * t3;
-    const double b4 = b1 + b2 + b3;
-    const double b5 = cav * (b2 - b3);
-    const double b6 = ruuav * (aq2 - r1 * aquu);
-    const double b7 = ruuav * (aq3 - r2 * aquu);
-    const double eplft = elft + plft, eprht = erht + prht;
-    // ---- reverse -------------------------------------------------------------
-    const double g0 = aj * fb[0], g1 = aj * fb[1], g2 = aj * fb[2], g3 = aj * fb[3];
+// Roe flux forward with every intermediate kept for the reverse sweep
+// (same arithmetic as roe_flux, src/model/flux.cpp:51-146).
+struct RoeTape {
+    double rlft, ulft, vlft, plft, rrht, urht, vrht, prht, r1, r2, aj;
+    double rlfti, rulft, rvlft, uvl, elft, hlft, rrhti, rurht, rvrht, uvr, erht, hrht;
+    double rat, rati, rav, uav, vav, hav, uv, cav, aq1, aq2, aq3, aq4, uu, c2, c2i, auu, aupc, aumc;
+    double uulft, uurht, rcav, aquu, c2ih, ruuav, t2, t3, b1, b2, b3, b4, b5, b6, b7, eplft, eprht;
+    double f[4];
+};
+
+__device__ inline void roe_fwd(RoeTape& t) {
+    t.rlfti = 1.0 / t.rlft;
+    t.rulft = t.rlft * t.ulft; t.rvlft = t.rlft * t.vlft;
+    t.uvl = 0.5 * (t.ulft * t.ulft + t.vlft * t.vlft);
+    t.elft = t.plft * OGM1 + t.rlft * t.uvl;
+    t.hlft = (t.elft + t.plft) * t.rlfti;
+    t.rrhti = 1.0 / t.rrht;
+    t.rurht = t.rrht * t.urht; t.rvrht = t.rrht * t.vrht;
+    t.uvr = 0.5 * (t.urht * t.urht + t.vrht * t.vrht);
+    t.erht = t.prht * OGM1 + t.rrht * t.uvr;
+    t.hrht = (t.erht + t.prht) * t.rrhti;
+    t.rat = ::sqrt(t.rrht * t.rlfti);
+    t.rati = 1.0 / (t.rat + 1.0);
+    t.rav = t.rat * t.rlft;
+    t.uav = (t.rat * t.urht + t.ulft) * t.rati;
+    t.vav = (t.rat * t.vrht + t.vlft) * t.rati;
+    t.hav = (t.rat * t.hrht + t.hlft) * t.rati;
+    t.uv = 0.5 * (t.uav * t.uav + t.vav * t.vav);
+    t.cav = ::sqrt(GM1 * (t.hav - t.uv));
+    t.aq1 = t.rrht - t.rlft; t.aq2 = t.urht - t.ulft; t.aq3 = t.vrht - t.vlft; t.aq4 = t.prht - t.plft;
+    t.uu = t.r1 * t.uav + t.r2 * t.vav;
+    t.c2 = t.cav * t.cav;
+    t.c2i = 1.0 / t.c2;
+    t.auu = ::fabs(t.uu); t.aupc = ::fabs(t.uu + t.cav); t.aumc = ::fabs(t.uu - t.cav);
+    t.uulft = t.r1 * t.ulft + t.r2 * t.vlft; t.uurht = t.r1 * t.urht + t.r2 * t.vrht;
+    t.rcav = t.rav * t.cav;
+    t.aquu = t.uurht - t.uulft;
+    t.c2ih = 0.5 * t.c2i;
+    t.ruuav = t.auu * t.rav;
+    t.t2 = t.aq4 + t.rcav * t.aquu; t.t3 = t.aq4 - t.rcav * t.aquu;
+    t.b1 = t.auu * (t.aq1 - t.c2i * t.aq4);
+    t.b2 = t.c2ih * t.aupc * t.t2;
+    t.b3 = t.c2ih * t.aumc * t.t3;
+    t.b4 = t.b1 + t.b2 + t.b3;
+    t.b5 = t.cav * (t.b2 - t.b3);
+    t.b6 = t.ruuav * (t.aq2 - t.r1 * t.aquu);
+    t.b7 = t.ruuav * (t.aq3 - t.r2 * t.aquu);
+    t.eplft = t.elft + t.plft; t.eprht = t.erht + t.prht;
+    const double d2 = t.uav * t.b4 + t.r1 * t.b5 + t.b6;
+    const double d3 = t.vav * t.b4 + t.r2 * t.b5 + t.b7;
+    const double d4 = t.hav * t.b4 + t.uu * t.b5 + t.uav * t.b6 + t.vav * t.b7 - t.c2 * t.b1 * OGM1;
+    const double plar = t.plft + t.prht;
+    t.f[0] = t.aj * (t.rlft * t.uulft + t.rrht * t.uurht - t.b4);
+    t.f[1] = t.aj * (t.rulft * t.uulft + t.rurht * t.uurht + t.r1 * plar - d2);
+    t.f[2] = t.aj * (t.rvlft * t.uulft + t.rvrht * t.uurht + t.r2 * plar - d3);
+    t.f[3] = t.aj * (t.eplft * t.uulft + t.eprht * t.uurht - d4);
+}
+
+// Reverse sweep: fb[0..3] = adjoint of f; accumulates the adjoints of the
+// eight face states into bl[0..3], br[0..3].
+__device__ inline void roe_rev(const RoeTape& t, const double* fb, double* bl, double* br) {
+    const double rlft = t.rlft, ulft = t.ulft, vlft = t.vlft, rrht = t.rrht, urht = t.urht, vrht = t.vrht;
+    const double r1 = t.r1, r2 = t.r2;
+    const double g0 = t.aj * fb[0], g1 = t.aj * fb[1], g2 = t.aj * fb[2], g3 = t.aj * fb[3];
     double rlft_ = 0, ulft_ = 0, vlft_ = 0, plft_ = 0, rrht_ = 0, urht_ = 0, vrht_ = 0, prht_ = 0;
     double uulft_ = 0, uurht_ = 0, rulft_ = 0, rurht_ = 0, rvlft_ = 0, rvrht_ = 0, eplft_ = 0, eprht_ = 0;
     double plar_ = 0;
-    rlft_ += g0 * uulft; uulft_ += g0 * rlft; rrht_ += g0 * uurht; uurht_ += g0 * rrht;
+    rlft_ += g0 * t.uulft; uulft_ += g0 * rlft; rrht_ += g0 * t.uurht; uurht_ += g0 * rrht;
     const double d1_ = -g0;
-    rulft_ += g1 * uulft; uulft_ += g1 * rulft; rurht_ += g1 * uurht; uurht_ += g1 * rurht; plar_ += g1 * r1;
+    rulft_ += g1 * t.uulft; uulft_ += g1 * t.rulft; rurht_ += g1 * t.uurht; uurht_ += g1 * t.rurht; plar_ += g1 * r1;
     const double d2_ = -g1;
-    rvlft_ += g2 * uulft; uulft_ += g2 * rvlft; rvrht_ += g2 * uurht; uurht_ += g2 * rvrht; plar_ += g2 * r2;
+    rvlft_ += g2 * t.uulft; uulft_ += g2 * t.rvlft; rvrht_ += g2 * t.uurht; uurht_ += g2 * t.rvrht; plar_ += g2 * r2;
     const double d3_ = -g2;
-    eplft_ += g3 * uulft; uulft_ += g3 * eplft; eprht_ += g3 * uurht; uurht_ += g3 * eprht;
+    eplft_ += g3 * t.uulft; uulft_ += g3 * t.eplft; eprht_ += g3 * t.uurht; uurht_ += g3 * t.eprht;
     const double d4_ = -g3;
     double elft_ = eplft_, erht_ = eprht_;
     plft_ += eplft_ + plar_;
     prht_ += eprht_ + plar_;
-    // d4 = hav b4 + uu b5 + uav b6 + vav b7 - c2 b1 OGM1
-    double hav_ = d4_ * b4, b4_ = d4_ * hav, uu_ = d4_ * b5, b5_ = d4_ * uu, uav_ = d4_ * b6, b6_ = d4_ * uav;
-    double vav_ = d4_ * b7, b7_ = d4_ * vav, c2_ = -d4_ * b1 * OGM1, b1_ = -d4_ * c2 * OGM1;
-    // d3 = vav b4 + r2 b5 + b7
-    vav_ += d3_ * b4; b4_ += d3_ * vav; b5_ += d3_ * r2; b7_ += d3_;
-    // d2 = uav b4 + r1 b5 + b6
-    uav_ += d2_ * b4; b4_ += d2_ * uav; b5_ += d2_ * r1; b6_ += d2_;
+    double hav_ = d4_ * t.b4, b4_ = d4_ * t.hav, uu_ = d4_ * t.b5, b5_ = d4_ * t.uu, uav_ = d4_ * t.b6, b6_ = d4_ * t.uav;
+    double vav_ = d4_ * t.b7, b7_ = d4_ * t.vav, c2_ = -d4_ * t.b1 * OGM1, b1_ = -d4_ * t.c2 * OGM1;
+    vav_ += d3_ * t.b4; b4_ += d3_ * t.vav; b5_ += d3_ * r2; b7_ += d3_;
+    uav_ += d2_ * t.b4; b4_ += d2_ * t.uav; b5_ += d2_ * r1; b6_ += d2_;
     b4_ += d1_;
-    double ruuav_ = b7_ * (aq3 - r2 * aquu) + b6_ * (aq2 - r1 * aquu);
-    double aq3_ = b7_ * ruuav, aq2_ = b6_ * ruuav;
-    double aquu_ = -b7_ * ruuav * r2 - b6_ * ruuav * r1;
-    double cav_ = b5_ * (b2 - b3);
-    double b2_ = b5_ * cav, b3_ = -b5_ * cav;
+    double ruuav_ = b7_ * (t.aq3 - r2 * t.aquu) + b6_ * (t.aq2 - r1 * t.aquu);
+    double aq3_ = b7_ * t.ruuav, aq2_ = b6_ * t.ruuav;
+    double aquu_ = -b7_ * t.ruuav * r2 - b6_ * t.ruuav * r1;
+    double cav_ = b5_ * (t.b2 - t.b3);
+    double b2_ = b5_ * t.cav, b3_ = -b5_ * t.cav;
     b1_ += b4_; b2_ += b4_; b3_ += b4_;
-    double c2ih_ = b3_ * aumc * t3 + b2_ * aupc * t2;
-    double aumc_ = b3_ * c2ih * t3, aupc_ = b2_ * c2ih * t2;
-    double aq4_ = b3_ * c2ih * aumc + b2_ * c2ih * aupc;
-    double rcav_ = -b3_ * c2ih * aumc * aquu + b2_ * c2ih * aupc * aquu;
-    aquu_ += -b3_ * c2ih * aumc * rcav + b2_ * c2ih * aupc * rcav;
-    double auu_ = b1_ * (aq1 - c2i * aq4);
-    double aq1_ = b1_ * auu;
-    double c2i_ = -b1_ * auu * aq4;
-    aq4_ += -b1_ * auu * c2i;
-    auu_ += ruuav_ * rav;
-    double rav_ = ruuav_ * auu;
+    double c2ih_ = b3_ * t.aumc * t.t3 + b2_ * t.aupc * t.t2;
+    double aumc_ = b3_ * t.c2ih * t.t3, aupc_ = b2_ * t.c2ih * t.t2;
+    double aq4_ = b3_ * t.c2ih * t.aumc + b2_ * t.c2ih * t.aupc;
+    double rcav_ = (b2_ * t.aupc - b3_ * t.aumc) * t.c2ih * t.aquu;
+    aquu_ += (b2_ * t.aupc - b3_ * t.aumc) * t.c2ih * t.rcav;
+    double auu_ = b1_ * (t.aq1 - t.c2i * t.aq4);
+    double aq1_ = b1_ * t.auu;
+    double c2i_ = -b1_ * t.auu * t.aq4;
+    aq4_ += -b1_ * t.auu * t.c2i;
+    auu_ += ruuav_ * t.rav;
+    double rav_ = ruuav_ * t.auu;
     c2i_ += 0.5 * c2ih_;
     uurht_ += aquu_; uulft_ -= aquu_;
-    rav_ += rcav_ * cav; cav_ += rcav_ * rav;
+    rav_ += rcav_ * t.cav; cav_ += rcav_ * t.rav;
     urht_ += uurht_ * r1; vrht_ += uurht_ * r2; ulft_ += uulft_ * r1; vlft_ += uulft_ * r2;
-    const double sm = sgn(uu - cav), sp = sgn(uu + cav), s0 = sgn(uu);
+    const double sm = sgn(t.uu - t.cav), sp = sgn(t.uu + t.cav), s0 = sgn(t.uu);
     uu_ += aumc_ * sm; cav_ -= aumc_ * sm;
     uu_ += aupc_ * sp; cav_ += aupc_ * sp;
     uu_ += auu_ * s0;
-    c2_ += -c2i_ * c2i * c2i;
-    cav_ += 2.0 * cav * c2_;
+    c2_ += -c2i_ * t.c2i * t.c2i;
+    cav_ += 2.0 * t.cav * c2_;
     uav_ += uu_ * r1; vav_ += uu_ * r2;
     rrht_ += aq1_; rlft_ -= aq1_; urht_ += aq2_; ulft_ -= aq2_; vrht_ += aq3_; vlft_ -= aq3_; prht_ += aq4_; plft_ -= aq4_;
     {
-        const double tmp = cav_ * GM1 * 0.5 / cav;
+        const double tmp = cav_ * GM1 * 0.5 / t.cav;
         hav_ += tmp;
-        const double uv_ = -tmp;
-        uav_ += uv_ * uav; vav_ += uv_ * vav;
+        uav_ -= tmp * t.uav; vav_ -= tmp * t.vav;
     }
     double rat_ = 0, rati_ = 0, hrht_ = 0, hlft_ = 0;
-    rat_ += hav_ * hrht * rati; hrht_ += hav_ * rat * rati; hlft_ += hav_ * rati; rati_ += hav_ * (rat * hrht + hlft);
-    rat_ += vav_ * vrht * rati; vrht_ += vav_ * rat * rati; vlft_ += vav_ * rati; rati_ += vav_ * (rat * vrht + vlft);
-    rat_ += uav_ * urht * rati; urht_ += uav_ * rat * rati; ulft_ += uav_ * rati; rati_ += uav_ * (rat * urht + ulft);
-    rat_ += rav_ * rlft; rlft_ += rav_ * rat;
-    rat_ += -rati_ * rati * rati;
+    rat_ += (hav_ * t.hrht + vav_ * vrht + uav_ * urht) * t.rati;
+    hrht_ += hav_ * t.rat * t.rati; hlft_ += hav_ * t.rati;
+    vrht_ += vav_ * t.rat * t.rati; vlft_ += vav_ * t.rati;
+    urht_ += uav_ * t.rat * t.rati; ulft_ += uav_ * t.rati;
+    rati_ += hav_ * (t.rat * t.hrht + t.hlft) + vav_ * (t.rat * vrht + vlft) + uav_ * (t.rat * urht + ulft);
+    rat_ += rav_ * rlft; rlft_ += rav_ * t.rat;
+    rat_ += -rati_ * t.rati * t.rati;
     double rlfti_ = 0, rrhti_ = 0;
     {
-        const double tmp = rat_ * 0.5 / rat;
-        rrht_ += tmp * rlfti; rlfti_ += tmp * rrht;
+        const double tmp = rat_ * 0.5 / t.rat;
+        rrht_ += tmp * t.rlfti; rlfti_ += tmp * rrht;
     }
-    erht_ += hrht_ * rrhti; prht_ += hrht_ * rrhti; rrhti_ += hrht_ * (erht + prht);
-    prht_ += erht_ * OGM1; rrht_ += erht_ * uvr;
+    erht_ += hrht_ * t.rrhti; prht_ += hrht_ * t.rrhti; rrhti_ += hrht_ * (t.erht + t.prht);
+    prht_ += erht_ * OGM1; rrht_ += erht_ * t.uvr;
     {
         const double uvr_ = erht_ * rrht;
         urht_ += uvr_ * urht; vrht_ += uvr_ * vrht;
     }
     rrht_ += rvrht_ * vrht + rurht_ * urht; vrht_ += rvrht_ * rrht; urht_ += rurht_ * rrht;
-    rrht_ += -rrhti_ * rrhti * rrhti;
-    elft_ += hlft_ * rlfti; plft_ += hlft_ * rlfti; rlfti_ += hlft_ * (elft + plft);
-    plft_ += elft_ * OGM1; rlft_ += elft_ * uvl;
+    rrht_ += -rrhti_ * t.rrhti * t.rrhti;
+    elft_ += hlft_ * t.rlfti; plft_ += hlft_ * t.rlfti; rlfti_ += hlft_ * (t.elft + t.plft);
+    plft_ += elft_ * OGM1; rlft_ += elft_ * t.uvl;
     {
         const double uvl_ = elft_ * rlft;
         ulft_ += uvl_ * ulft; vlft_ += uvl_ * vlft;
     }
     rlft_ += rvlft_ * vlft + rulft_ * ulft; vlft_ += rvlft_ * rlft; ulft_ += rulft_ * rlft;
-    rlft_ += -rlfti_ * rlfti * rlfti;
+    rlft_ += -rlfti_ * t.rlfti * t.rlfti;
     bl[0] += rlft_; bl[1] += ulft_; bl[2] += vlft_; bl[3] += plft_;
     br[0] += rrht_; br[1] += urht_; br[2] += vrht_; br[3] += prht_;
 }
 
 // Reverse of sa_source (same forward formulas); outputs adjoints of rho, nut,
 // mu, omega, |grad nut|^2 and beta for source adjoint sb.
-__device__ inline void sa_source_adj(double rho, double nut, double mu, double d, double omega, double gnut2,
-                                     double beta, double sb, double* rho_, double* nut_, double* mu_,
-                                     double* omega_, double* gnut2_, double* beta_) {
+__device__ inline double sa_source_adj(double rho, double nut, double mu, double d, double omega, double gnut2,
+                                       double beta, double sb, double* rho_, double* nut_, double* mu_,
+                                       double* omega_, double* gnut2_, double* beta_) {
     const double k2d2 = SA_KAPPA * SA_KAPPA * d * d;
     const double chi = rho * nut / mu;
     const double chi3 = chi * chi * chi;
@@ -242,6 +265,7 @@ __device__ inline void sa_source_adj(double rho, double nut, double mu, double d
     *rho_ = rhob;
     *nut_ = nutb;
     *omega_ = omegab;
+    return rho * (prod - dest) + (SA_CB2 / SA_SIGMA) * rho * gnut2;
 }
 
 // SA only: face gradient parts (u_y, v_x, nut_x, nut_y) the cell source needs.
@@ -265,60 +289,52 @@ __global__ void __launch_bounds__(256) k_face_grad(DevCase c, const double* __re
     }
 }
 
-// R1: adjoint weights w = psi / V per cell, and the SA source adjoint.
-template <int NQ>
-__global__ void __launch_bounds__(256) k_cell_adj(DevCase c, const double* __restrict__ P, const double* __restrict__ Gi,
+// R1 (SA): the cell source, forward and reverse.  rhs_4 = (... + S V) / V,
+// so the source adjoint is psi_4 (V/V).  Writes the source value, the
+// adjoints of the cell's own rho, nut, mu, and of the four face gradient parts
+// it averages (the same for all four faces), and (dR/dbeta)^T psi.
+__global__ void __launch_bounds__(256) k_cell_src(DevCase c, const double* __restrict__ P, const double* __restrict__ Gi,
                                                   const double* __restrict__ Gj, const double* __restrict__ beta,
-                                                  const double* __restrict__ psi, double* __restrict__ w,
-                                                  double* __restrict__ srec, double* __restrict__ outb) {
+                                                  const double* __restrict__ psi, double* __restrict__ srec,
+                                                  double* __restrict__ outb) {
     const size_t n = (size_t)c.nic * c.njc;
     for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += (size_t)gridDim.x * blockDim.x) {
         const int i = (int)(idx / c.njc), j = (int)(idx % c.njc);
-        const double iv = c.ivol[idx];
-#pragma unroll
-        for (int k = 0; k < NQ; k++) w[idx * NQ + k] = psi[idx * NQ + k] * iv;
-        if (NQ == 5) {
-            double* s = srec + idx * SRW;
-            double bb = 0.0;
-            if (c.viscous) {
-                const double* gw = Gi + ((size_t)i * c.njc + j) * 4;
-                const double* ge = Gi + ((size_t)(i + 1) * c.njc + j) * 4;
-                const double* gs = Gj + ((size_t)i * c.nj + j) * 4;
-                const double* gn = Gj + ((size_t)i * c.nj + j + 1) * 4;
-                const double uy = 0.25 * (gw[0] + ge[0] + gs[0] + gn[0]);
-                const double vx = 0.25 * (gw[1] + ge[1] + gs[1] + gn[1]);
-                const double nx = 0.25 * (gw[2] + ge[2] + gs[2] + gn[2]);
-                const double ny = 0.25 * (gw[3] + ge[3] + gs[3] + gn[3]);
-                const double om = ::fabs(vx - uy);
-                const double* pc = P + pidx(c, i + 1, j + 1);
-                const double bt = beta ? beta[idx] : 1.0;
-                // rhs_4 = (... + S V) / V, so dJ/dS = psi_4 (V/V)
-                const double sb = psi[idx * NQ + 4] * (c.vol[idx] * iv);
-                double rho_, nut_, mu_, om_, g2_, b_;
-                sa_source_adj(pc[P_RHO], pc[P_NUT], pc[P_MU], c.wd[idx], om, nx * nx + ny * ny, bt, sb, &rho_, &nut_,
-                              &mu_, &om_, &g2_, &b_);
-                const double sg = sgn(vx - uy);
-                s[S_GU] = 0.25 * (-om_ * sg);
-                s[S_GV] = 0.25 * (om_ * sg);
-                s[S_GNX] = 0.25 * (2.0 * nx * g2_);
-                s[S_GNY] = 0.25 * (2.0 * ny * g2_);
-                s[S_RHO] = rho_; s[S_NUT] = nut_; s[S_MU] = mu_;
-                bb = b_;
-            } else {
-                for (int k = 0; k < SRW; k++) s[k] = 0.0;
-            }
-            if (outb) outb[idx] = bb;
-        }
+        const double* gw = Gi + ((size_t)i * c.njc + j) * 4;
+        const double* ge = Gi + ((size_t)(i + 1) * c.njc + j) * 4;
+        const double* gs = Gj + ((size_t)i * c.nj + j) * 4;
+        const double* gn = Gj + ((size_t)i * c.nj + j + 1) * 4;
+        const double uy = 0.25 * (gw[0] + ge[0] + gs[0] + gn[0]);
+        const double vx = 0.25 * (gw[1] + ge[1] + gs[1] + gn[1]);
+        const double nx = 0.25 * (gw[2] + ge[2] + gs[2] + gn[2]);
+        const double ny = 0.25 * (gw[3] + ge[3] + gs[3] + gn[3]);
+        const double om = ::fabs(vx - uy);
+        const double* pc = P + pidx(c, i + 1, j + 1);
+        const double bt = beta ? beta[idx] : 1.0;
+        const double sb = psi ? psi[idx * 5 + 4] * (c.vol[idx] * c.ivol[idx]) : 0.0;
+        double rho_, nut_, mu_, om_, g2_, b_;
+        const double S = sa_source_adj(pc[P_RHO], pc[P_NUT], pc[P_MU], c.wd[idx], om, nx * nx + ny * ny, bt, sb, &rho_,
+                                       &nut_, &mu_, &om_, &g2_, &b_);
+        const double sg = sgn(vx - uy);
+        double* s = srec + idx * SRW;
+        s[S_GU] = 0.25 * (-om_ * sg);
+        s[S_GV] = 0.25 * (om_ * sg);
+        s[S_GNX] = 0.25 * (2.0 * nx * g2_);
+        s[S_GNY] = 0.25 * (2.0 * ny * g2_);
+        s[S_RHO] = rho_; s[S_NUT] = nut_; s[S_MU] = mu_; s[S_VAL] = S;
+        if (outb) outb[idx] = b_;
     }
 }
 
-// R2: per face, recompute the flux and run its adjoint.  Seed: the flux
-// adjoint w(R) - w(L) (ghost sides 0) and, with SA, the gradient-part
-// adjoints of the two adjacent cells' sources.
+// R2: one pass per face family that computes the face flux (for the
+// residual, when F != nullptr) and runs its reverse sweep in place, seeded by
+// the flux adjoint w(R) - w(L), w = psi / V (0 on ghost sides), and, with SA,
+// by the gradient-part adjoints of the two adjacent cells' sources.
 template <int NQ, int DIR, int ORDER>
-__global__ void __launch_bounds__(256) k_face_adj(DevCase c, const double* __restrict__ P, const double* __restrict__ phi,
-                                                  const double* __restrict__ w, const double* __restrict__ srec,
-                                                  double* __restrict__ arec) {
+__global__ void __launch_bounds__(256) k_face_fused(DevCase c, const double* __restrict__ P,
+                                                    const double* __restrict__ lim, const double* __restrict__ psi,
+                                                    const double* __restrict__ srec, double* __restrict__ F,
+                                                    double* __restrict__ arec) {
     const int na = DIR == 0 ? c.ni : c.nic;
     const int nb = DIR == 0 ? c.njc : c.nj;
     const size_t n = (size_t)na * nb;
@@ -331,44 +347,42 @@ __global__ void __launch_bounds__(256) k_face_adj(DevCase c, const double* __res
         const double* pL = P + fi.L;
         const double* pR = P + fi.R;
         double* o = arec + fi.face * ARW;
-        // flux seed
         double fb[5];
+        {
+            const double ivr = fi.limR ? c.ivol[fi.phR] : 0.0, ivl = fi.limL ? c.ivol[fi.phL] : 0.0;
 #pragma unroll
-        for (int k = 0; k < NQ; k++) {
-            const double wr = fi.limR ? w[fi.phR * NQ + k] : 0.0;
-            const double wl = fi.limL ? w[fi.phL * NQ + k] : 0.0;
-            fb[k] = wr - wl;
+            for (int k = 0; k < NQ; k++) {
+                const double wr = fi.limR ? psi[fi.phR * NQ + k] * ivr : 0.0;
+                const double wl = fi.limL ? psi[fi.phL * NQ + k] * ivl : 0.0;
+                fb[k] = wr - wl;
+            }
         }
-        // face states
         double qL[5], qR[5];
 #pragma unroll
         for (int k = 0; k < NQ; k++) {
-            const int m = slot[k];
-            qL[k] = pL[m];
-            qR[k] = pR[m];
+            qL[k] = pL[slot[k]];
+            qR[k] = pR[slot[k]];
             if (ORDER == 2) {
-                const double dC = pR[m] - pL[m];
-                if (fi.limL) qL[k] += phi[fi.phL * NQ + k] * (THM * (pL[m] - P[fi.LL + m]) + THP * dC);
-                if (fi.limR) qR[k] -= phi[fi.phR * NQ + k] * (THP * dC + THM * (P[fi.RR + m] - pR[m]));
+                if (fi.limL) qL[k] += lim[lim_off(c, DIR, LIM_SL, fi.phL) + k];
+                if (fi.limR) qR[k] -= lim[lim_off(c, DIR, LIM_SR, fi.phR) + k];
             }
         }
+        RoeTape rt;
+        rt.rlft = qL[0]; rt.ulft = qL[1]; rt.vlft = qL[2]; rt.plft = qL[3];
+        rt.rrht = qR[0]; rt.urht = qR[1]; rt.vrht = qR[2]; rt.prht = qR[3];
+        rt.r1 = gm[G_R1]; rt.r2 = gm[G_R2]; rt.aj = gm[G_AJ];
+        roe_fwd(rt);
+        double f[5] = {rt.f[0], rt.f[1], rt.f[2], rt.f[3], 0.0};
         double bl[5] = {0, 0, 0, 0, 0}, br[5] = {0, 0, 0, 0, 0};
-        double fc0b = fb[0];
+        double fcb[4] = {fb[0], fb[1], fb[2], fb[3]};
         if (NQ == 5) {
-            // f4 = f0 * nut_upwind
-            double f[4];
-            roe_flux<double>(qL[0], qL[1], qL[2], qL[3], qR[0], qR[1], qR[2], qR[3], gm[G_R1], gm[G_R2], gm[G_AJ], f);
-            const bool up = f[0] >= 0.0;
+            const bool up = rt.f[0] >= 0.0;
             const double nup = up ? qL[4] : qR[4];
-            fc0b += fb[4] * nup;
-            if (up) bl[4] += fb[4] * f[0]; else br[4] += fb[4] * f[0];
+            f[4] = rt.f[0] * nup;
+            fcb[0] += fb[4] * nup;
+            if (up) bl[4] += fb[4] * rt.f[0]; else br[4] += fb[4] * rt.f[0];
         }
-        {
-            const double fcb[4] = {fc0b, fb[1], fb[2], fb[3]};
-            roe_flux_adj(qL[0], qL[1], qL[2], qL[3], qR[0], qR[1], qR[2], qR[3], gm[G_R1], gm[G_R2], gm[G_AJ], fcb, bl, br);
-        }
-#pragma unroll
-        for (int k = 0; k < 5; k++) { o[A_QL + k] = bl[k]; o[A_QR + k] = br[k]; }
+        roe_rev(rt, fcb, bl, br);
         if (c.viscous) {
             const double* pPa = P + fi.Pa; const double* pPb = P + fi.Pb;
             const double* pMa = P + fi.Ma; const double* pMb = P + fi.Mb;
@@ -400,24 +414,28 @@ __global__ void __launch_bounds__(256) k_face_adj(DevCase c, const double* __res
             const double txy = mu * (dudy + dvdx);
             const double txx = mu * (2.0 * dudx - 2.0 / 3.0 * div);
             const double tyy = mu * (2.0 * dvdy - 2.0 / 3.0 * div);
-            // F_net = F_conv - F_visc
+            // forward viscous flux (for the residual)
+            f[1] -= txx * nx + txy * ny;
+            f[2] -= txy * nx + tyy * ny;
+            f[3] -= (ub * txx + vb * txy + k * dTdx) * nx + (ub * txy + vb * tyy + k * dTdy) * ny;
+            // reverse; F_net = F_conv - F_visc
             const double v1 = -fb[1], v2 = -fb[2], v3 = -fb[3];
             const double A_ = v3 * nx, B_ = v3 * ny;
             const double ub_ = A_ * txx + B_ * txy;
             const double vb_ = A_ * txy + B_ * tyy;
-            double txx_ = A_ * ub + v1 * nx;
-            double txy_ = A_ * vb + B_ * ub + v2 * nx + v1 * ny;
-            double tyy_ = B_ * vb + v2 * ny;
-            const double qx_ = -A_, qy_ = -B_;
-            const double k_ = -qx_ * dTdx - qy_ * dTdy;
-            const double dTdx_ = -qx_ * k, dTdy_ = -qy_ * k;
-            double mu_ = tyy_ * (2.0 * dvdy - 2.0 / 3.0 * div) + txx_ * (2.0 * dudx - 2.0 / 3.0 * div) + txy_ * (dudy + dvdx);
+            const double txx_ = A_ * ub + v1 * nx;
+            const double txy_ = A_ * vb + B_ * ub + v2 * nx + v1 * ny;
+            const double tyy_ = B_ * vb + v2 * ny;
+            const double k_ = A_ * dTdx + B_ * dTdy;
+            const double dTdx_ = A_ * k, dTdy_ = B_ * k;
+            const double mu_ = tyy_ * (2.0 * dvdy - 2.0 / 3.0 * div) + txx_ * (2.0 * dudx - 2.0 / 3.0 * div)
+                             + txy_ * (dudy + dvdx);
             double dvdy_ = tyy_ * mu * 2.0, dudx_ = txx_ * mu * 2.0;
             const double div_ = -(tyy_ + txx_) * mu * (2.0 / 3.0);
             double dudy_ = txy_ * mu, dvdx_ = txy_ * mu;
             dudx_ += div_; dvdy_ += div_;
             double mub_ = mu_, mutb_ = 0.0;
-            if (NQ == 5) { mutb_ = mu_; mub_ += k_ * c.cp / c.pr; mutb_ += k_ * c.cp / PR_TURB; }
+            if (NQ == 5) { mutb_ = mu_ + k_ * c.cp / PR_TURB; mub_ += k_ * c.cp / c.pr; }
             else mub_ += k_ * (c.cp / c.pr);
             o[A_DTDX] = dTdx_; o[A_DTDY] = dTdy_;
             o[A_UB] = ub_; o[A_VB] = vb_;
@@ -428,18 +446,16 @@ __global__ void __launch_bounds__(256) k_face_adj(DevCase c, const double* __res
                 const double rnb = 0.375 * (pL[P_RHO] * pL[P_NUT] + pR[P_RHO] * pR[P_NUT])
                                  + 0.0625 * (pPa[P_RHO] * pPa[P_NUT] + pPb[P_RHO] * pPb[P_NUT]
                                              + pMa[P_RHO] * pMa[P_NUT] + pMb[P_RHO] * pMb[P_NUT]);
-                const double v4 = -fb[4];
                 const double cs = 1.0 / SA_SIGMA;
                 const double gdn = dndx * nx + dndy * ny;
+                f[4] -= cs * (mub + rnb) * gdn;
+                const double v4 = -fb[4];
                 mub_ += v4 * cs * gdn;
                 const double rnb_ = v4 * cs * gdn;
                 double dndx_ = v4 * cs * (mub + rnb) * nx, dndy_ = v4 * cs * (mub + rnb) * ny;
-                // cell-source seeds on this face's gradient parts
-                const double* sl = fi.limL ? srec + fi.phL * SRW : nullptr;
-                const double* sr = fi.limR ? srec + fi.phR * SRW : nullptr;
                 double gs[4] = {0, 0, 0, 0};
-                if (sl) for (int t = 0; t < 4; t++) gs[t] += sl[t];
-                if (sr) for (int t = 0; t < 4; t++) gs[t] += sr[t];
+                if (fi.limL) { const double* sl = srec + fi.phL * SRW; for (int t = 0; t < 4; t++) gs[t] += sl[t]; }
+                if (fi.limR) { const double* sr = srec + fi.phR * SRW; for (int t = 0; t < 4; t++) gs[t] += sr[t]; }
                 dudy_ += gs[0]; dvdx_ += gs[1]; dndx_ += gs[2]; dndy_ += gs[3];
                 o[A_DNDX] = dndx_; o[A_DNDY] = dndy_; o[A_RNB] = rnb_;
             } else {
@@ -451,56 +467,66 @@ __global__ void __launch_bounds__(256) k_face_adj(DevCase c, const double* __res
         } else {
             for (int t = A_DUDX; t <= A_RNB; t++) o[t] = 0.0;
         }
-    }
-}
-
-// R3: limiter adjoint per physical cell and direction.  For cell c the
-// limited states are qL(c's high face) = P + phi (THM d- + THP d+) and
-// qR(c's low face) = P - phi (THP d- + THM d+) with d- = P(c)-P(c-1),
-// d+ = P(c+1)-P(c).  Writes (dbar-, dbar+) per component.
-template <int NQ>
-__global__ void __launch_bounds__(256) k_limiter_adj(DevCase c, const double* __restrict__ P,
-                                                     const double* __restrict__ phi_i, const double* __restrict__ phi_j,
-                                                     const double* __restrict__ ai, const double* __restrict__ aj,
-                                                     double* __restrict__ lrec) {
-    const size_t n = (size_t)c.nic * c.njc;
-    const int slot[5] = {P_RHO, P_U, P_V, P_P, P_NUT};
-    for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += (size_t)gridDim.x * blockDim.x) {
-        const int i = (int)(idx / c.njc), j = (int)(idx % c.njc);
-        const double* pc = P + pidx(c, i + 1, j + 1);
+        // reconstruction reverse: direct terms and the slopes' d-, d+ parts
 #pragma unroll
-        for (int dir = 0; dir < 2; dir++) {
-            const double* pm = dir == 0 ? P + pidx(c, i, j + 1) : P + pidx(c, i + 1, j);
-            const double* pp = dir == 0 ? P + pidx(c, i + 2, j + 1) : P + pidx(c, i + 1, j + 2);
-            const double* phi = dir == 0 ? phi_i : phi_j;
-            const double eps = dir == 0 ? c.eps_chi : c.eps_eta;
-            // adjoint records of the high face (c is its L) and low face (c is its R)
-            const double* hi = dir == 0 ? ai + ((size_t)(i + 1) * c.njc + j) * ARW : aj + ((size_t)i * c.nj + j + 1) * ARW;
-            const double* lo = dir == 0 ? ai + ((size_t)i * c.njc + j) * ARW : aj + ((size_t)i * c.nj + j) * ARW;
-            double* out = lrec + (idx * 2 + dir) * 2 * NQ;
-#pragma unroll
-            for (int k = 0; k < NQ; k++) {
-                const int m = slot[k];
-                const double fa = pc[m] - pm[m], fb = pp[m] - pc[m];
-                const double ph = phi[idx * NQ + k];
-                const double A = hi[A_QL + k], B = lo[A_QR + k];
-                const double phb = A * (THM * fa + THP * fb) - B * (THP * fa + THM * fb);
-                const double a2e = 2.0 * (fb - fa) * (fb - fa) + 3.0 * fb * fa + eps;
-                const double dphi_dfa = (0.75 * fb - ph * (-4.0 * (fb - fa) + 3.0 * fb)) / a2e;
-                const double dphi_dfb = (0.75 * fa - ph * (4.0 * (fb - fa) + 3.0 * fa)) / a2e;
-                out[k] = A * ph * THM - B * ph * THP + phb * dphi_dfa;        // dbar-
-                out[NQ + k] = A * ph * THP - B * ph * THM + phb * dphi_dfb;   // dbar+
+        for (int k = 0; k < 5; k++) {
+            const bool kk = k < NQ;
+            const double A = kk ? bl[k] : 0.0, B = kk ? br[k] : 0.0;
+            o[A_AL + k] = A;
+            o[A_BR + k] = B;
+            double dml = 0.0, dpl = 0.0, dmr = 0.0, dpr = 0.0;
+            if (ORDER == 2 && kk) {
+                if (fi.limL) {
+                    dml = A * lim[lim_off(c, DIR, LIM_AM, fi.phL) + k];
+                    dpl = A * lim[lim_off(c, DIR, LIM_AP, fi.phL) + k];
+                }
+                if (fi.limR) {
+                    dmr = -B * lim[lim_off(c, DIR, LIM_BM, fi.phR) + k];
+                    dpr = -B * lim[lim_off(c, DIR, LIM_BP, fi.phR) + k];
+                }
             }
+            o[A_DML + k] = dml; o[A_DPL + k] = dpl; o[A_DMR + k] = dmr; o[A_DPR + k] = dpr;
+        }
+        if (F) {
+            double* fo = F + fi.face * NQ;
+#pragma unroll
+            for (int k = 0; k < NQ; k++) fo[k] = f[k];
         }
     }
 }
 
-// R4: gather the adjoint of every ghost-padded primitive record from the
-// faces whose stencils contain it.
+// Residual assembly from precomputed face fluxes and (SA) source values.
+template <int NQ>
+__global__ void __launch_bounds__(256) k_cell_res(DevCase c, const double* __restrict__ Fi, const double* __restrict__ Fj,
+                                                  const double* __restrict__ srec, double* __restrict__ rhs) {
+    const size_t n = (size_t)c.nic * c.njc;
+    for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += (size_t)gridDim.x * blockDim.x) {
+        const int i = (int)(idx / c.njc), j = (int)(idx % c.njc);
+        const double* fs = Fj + ((size_t)i * c.nj + j) * NQ;
+        const double* fn = fs + NQ;
+        const double* fw = Fi + ((size_t)i * c.njc + j) * NQ;
+        const double* fe = Fi + ((size_t)(i + 1) * c.njc + j) * NQ;
+        double r[NQ];
+#pragma unroll
+        for (int k = 0; k < NQ; k++) r[k] = (fs[k] - fn[k]) + (fw[k] - fe[k]);
+        const double vol = c.vol[idx];
+        if (NQ == 5 && c.viscous) r[NQ - 1] += srec[idx * SRW + S_VAL] * vol;
+        r[1] += -c.dpdx * vol;
+        r[2] += -c.dpdy * vol;
+        const double iv = c.ivol[idx];
+#pragma unroll
+        for (int k = 0; k < NQ; k++) rhs[idx * NQ + k] = r[k] * iv;
+    }
+}
+
+// R3: gather the adjoint of every ghost-padded primitive record from the
+// faces whose stencils contain it: the two faces it is a side of (direct and
+// slope parts), the faces of its two neighbours along each direction (their
+// slopes depend on this cell), and the six viscous stencils per direction.
 template <int NQ, int ORDER>
 __global__ void __launch_bounds__(256) k_gather(DevCase c, const double* __restrict__ P, const double* __restrict__ ai,
-                                                const double* __restrict__ aj, const double* __restrict__ lrec,
-                                                const double* __restrict__ srec, double* __restrict__ Pbar) {
+                                                const double* __restrict__ aj, const double* __restrict__ srec,
+                                                double* __restrict__ Pbar) {
     const size_t n = (size_t)(c.nic + 2) * (c.njc + 2);
     const int slot[5] = {P_RHO, P_U, P_V, P_P, P_NUT};
     for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += (size_t)gridDim.x * blockDim.x) {
@@ -508,120 +534,94 @@ __global__ void __launch_bounds__(256) k_gather(DevCase c, const double* __restr
         double acc[NP];
 #pragma unroll
         for (int s = 0; s < NP; s++) acc[s] = 0.0;
-        const bool phys = ip >= 1 && ip <= c.nic && jp >= 1 && jp <= c.njc;
         const double* self = P + idx * NP;
+        auto visc = [&](const double* r, const double* gm, int role) {
+            double wx, wy, co;
+            if (role == 0) { wx = gm[G_WLX]; wy = gm[G_WLY]; co = 0.375; }
+            else if (role == 1) { wx = gm[G_WRX]; wy = gm[G_WRY]; co = 0.375; }
+            else if (role == 2) { wx = gm[G_WPX]; wy = gm[G_WPY]; co = 0.0625; }
+            else { wx = gm[G_WMX]; wy = gm[G_WMY]; co = 0.0625; }
+            acc[P_U] += r[A_DUDX] * wx + r[A_DUDY] * wy + r[A_UB] * co;
+            acc[P_V] += r[A_DVDX] * wx + r[A_DVDY] * wy + r[A_VB] * co;
+            acc[P_T] += r[A_DTDX] * wx + r[A_DTDY] * wy;
+            acc[P_MU] += r[A_MUB] * co;
+            if (NQ == 5) {
+                acc[P_MUT] += r[A_MUTB] * co;
+                acc[P_NUT] += r[A_DNDX] * wx + r[A_DNDY] * wy + r[A_RNB] * co * self[P_RHO];
+                acc[P_RHO] += r[A_RNB] * co * self[P_NUT];
+            }
+        };
         // ---- i-faces (f, j): L=(f, j+1) R=(f+1, j+1) P=(f|f+1, j+2) M=(f|f+1, j)
         {
-            auto visc = [&](int f, int j, int role) {
-                if (f < 0 || f > c.nic || j < 0 || j >= c.njc) return;
-                const size_t fid = (size_t)f * c.njc + j;
-                const double* r = ai + fid * ARW;
-                const double* gm = c.geo_i + fid * NGEO;
-                double wx, wy, co;
-                if (role == 0) { wx = gm[G_WLX]; wy = gm[G_WLY]; co = 0.375; }
-                else if (role == 1) { wx = gm[G_WRX]; wy = gm[G_WRY]; co = 0.375; }
-                else if (role == 2) { wx = gm[G_WPX]; wy = gm[G_WPY]; co = 0.0625; }
-                else { wx = gm[G_WMX]; wy = gm[G_WMY]; co = 0.0625; }
-                acc[P_U] += r[A_DUDX] * wx + r[A_DUDY] * wy + r[A_UB] * co;
-                acc[P_V] += r[A_DVDX] * wx + r[A_DVDY] * wy + r[A_VB] * co;
-                acc[P_T] += r[A_DTDX] * wx + r[A_DTDY] * wy;
-                acc[P_MU] += r[A_MUB] * co;
-                if (NQ == 5) {
-                    acc[P_MUT] += r[A_MUTB] * co;
-                    acc[P_NUT] += r[A_DNDX] * wx + r[A_DNDY] * wy + r[A_RNB] * co * self[P_RHO];
-                    acc[P_RHO] += r[A_RNB] * co * self[P_NUT];
-                }
+            auto rec = [&](int f, int j) -> const double* {
+                return (f < 0 || f > c.nic || j < 0 || j >= c.njc) ? nullptr : ai + ((size_t)f * c.njc + j) * ARW;
             };
             if (jp >= 1 && jp <= c.njc) {
                 const int j = jp - 1;
-                if (ip <= c.nic) {  // L of face ip
-                    const double* r = ai + ((size_t)ip * c.njc + j) * ARW;
-                    for (int k = 0; k < NQ; k++) acc[slot[k]] += r[A_QL + k];
-                }
-                if (ip >= 1) {  // R of face ip-1
-                    const double* r = ai + ((size_t)(ip - 1) * c.njc + j) * ARW;
-                    for (int k = 0; k < NQ; k++) acc[slot[k]] += r[A_QR + k];
-                }
-                if (ORDER == 2) {
-                    if (phys) {
-                        const double* l = lrec + (((size_t)(ip - 1) * c.njc + j) * 2 + 0) * 2 * NQ;
-                        for (int k = 0; k < NQ; k++) acc[slot[k]] += l[k] - l[NQ + k];
+                const double* f0 = rec(ip, j);       // this cell is its L
+                const double* f1 = rec(ip - 1, j);   // this cell is its R
+                for (int k = 0; k < NQ; k++) {
+                    double s = 0.0;
+                    if (f0) s += f0[A_AL + k];
+                    if (f1) s += f1[A_BR + k];
+                    if (ORDER == 2) {
+                        const double* fm2 = rec(ip - 2, j);
+                        const double* fp1 = rec(ip + 1, j);
+                        if (f0) s += f0[A_DML + k] - f0[A_DPL + k] - f0[A_DMR + k];
+                        if (f1) s += f1[A_DMR + k] - f1[A_DPR + k] + f1[A_DPL + k];
+                        if (fm2) s += fm2[A_DPR + k];
+                        if (fp1) s -= fp1[A_DML + k];
                     }
-                    if (ip - 1 >= 1 && ip - 1 <= c.nic) {  // left neighbour is physical: +dbar+
-                        const double* l = lrec + (((size_t)(ip - 2) * c.njc + j) * 2 + 0) * 2 * NQ;
-                        for (int k = 0; k < NQ; k++) acc[slot[k]] += l[NQ + k];
-                    }
-                    if (ip + 1 >= 1 && ip + 1 <= c.nic) {  // right neighbour is physical: -dbar-
-                        const double* l = lrec + (((size_t)ip * c.njc + j) * 2 + 0) * 2 * NQ;
-                        for (int k = 0; k < NQ; k++) acc[slot[k]] -= l[k];
-                    }
+                    acc[slot[k]] += s;
                 }
             }
             if (c.viscous) {
-                visc(ip, jp - 1, 0);       // L
-                visc(ip - 1, jp - 1, 1);   // R
-                visc(ip, jp - 2, 2);       // P, low
-                visc(ip - 1, jp - 2, 2);   // P, high
-                visc(ip, jp, 3);           // M, low
-                visc(ip - 1, jp, 3);       // M, high
+                const int fs[6] = {ip, ip - 1, ip, ip - 1, ip, ip - 1};
+                const int js[6] = {jp - 1, jp - 1, jp - 2, jp - 2, jp, jp};
+                const int roles[6] = {0, 1, 2, 2, 3, 3};
+#pragma unroll
+                for (int t = 0; t < 6; t++) {
+                    const double* r = rec(fs[t], js[t]);
+                    if (r) visc(r, c.geo_i + ((size_t)fs[t] * c.njc + js[t]) * NGEO, roles[t]);
+                }
             }
         }
         // ---- j-faces (i, g): L=(i+1, g) R=(i+1, g+1) P=(i+2, g|g+1) M=(i, g|g+1)
         {
-            auto visc = [&](int i, int g, int role) {
-                if (i < 0 || i >= c.nic || g < 0 || g > c.njc) return;
-                const size_t fid = (size_t)i * c.nj + g;
-                const double* r = aj + fid * ARW;
-                const double* gm = c.geo_j + fid * NGEO;
-                double wx, wy, co;
-                if (role == 0) { wx = gm[G_WLX]; wy = gm[G_WLY]; co = 0.375; }
-                else if (role == 1) { wx = gm[G_WRX]; wy = gm[G_WRY]; co = 0.375; }
-                else if (role == 2) { wx = gm[G_WPX]; wy = gm[G_WPY]; co = 0.0625; }
-                else { wx = gm[G_WMX]; wy = gm[G_WMY]; co = 0.0625; }
-                acc[P_U] += r[A_DUDX] * wx + r[A_DUDY] * wy + r[A_UB] * co;
-                acc[P_V] += r[A_DVDX] * wx + r[A_DVDY] * wy + r[A_VB] * co;
-                acc[P_T] += r[A_DTDX] * wx + r[A_DTDY] * wy;
-                acc[P_MU] += r[A_MUB] * co;
-                if (NQ == 5) {
-                    acc[P_MUT] += r[A_MUTB] * co;
-                    acc[P_NUT] += r[A_DNDX] * wx + r[A_DNDY] * wy + r[A_RNB] * co * self[P_RHO];
-                    acc[P_RHO] += r[A_RNB] * co * self[P_NUT];
-                }
+            auto rec = [&](int i, int g) -> const double* {
+                return (i < 0 || i >= c.nic || g < 0 || g > c.njc) ? nullptr : aj + ((size_t)i * c.nj + g) * ARW;
             };
             if (ip >= 1 && ip <= c.nic) {
                 const int i = ip - 1;
-                if (jp <= c.njc) {  // L of face jp
-                    const double* r = aj + ((size_t)i * c.nj + jp) * ARW;
-                    for (int k = 0; k < NQ; k++) acc[slot[k]] += r[A_QL + k];
-                }
-                if (jp >= 1) {  // R of face jp-1
-                    const double* r = aj + ((size_t)i * c.nj + jp - 1) * ARW;
-                    for (int k = 0; k < NQ; k++) acc[slot[k]] += r[A_QR + k];
-                }
-                if (ORDER == 2) {
-                    if (phys) {
-                        const double* l = lrec + (((size_t)i * c.njc + jp - 1) * 2 + 1) * 2 * NQ;
-                        for (int k = 0; k < NQ; k++) acc[slot[k]] += l[k] - l[NQ + k];
+                const double* f0 = rec(i, jp);
+                const double* f1 = rec(i, jp - 1);
+                for (int k = 0; k < NQ; k++) {
+                    double s = 0.0;
+                    if (f0) s += f0[A_AL + k];
+                    if (f1) s += f1[A_BR + k];
+                    if (ORDER == 2) {
+                        const double* fm2 = rec(i, jp - 2);
+                        const double* fp1 = rec(i, jp + 1);
+                        if (f0) s += f0[A_DML + k] - f0[A_DPL + k] - f0[A_DMR + k];
+                        if (f1) s += f1[A_DMR + k] - f1[A_DPR + k] + f1[A_DPL + k];
+                        if (fm2) s += fm2[A_DPR + k];
+                        if (fp1) s -= fp1[A_DML + k];
                     }
-                    if (jp - 1 >= 1 && jp - 1 <= c.njc) {
-                        const double* l = lrec + (((size_t)i * c.njc + jp - 2) * 2 + 1) * 2 * NQ;
-                        for (int k = 0; k < NQ; k++) acc[slot[k]] += l[NQ + k];
-                    }
-                    if (jp + 1 >= 1 && jp + 1 <= c.njc) {
-                        const double* l = lrec + (((size_t)i * c.njc + jp) * 2 + 1) * 2 * NQ;
-                        for (int k = 0; k < NQ; k++) acc[slot[k]] -= l[k];
-                    }
+                    acc[slot[k]] += s;
                 }
             }
             if (c.viscous) {
-                visc(ip - 1, jp, 0);       // L
-                visc(ip - 1, jp - 1, 1);   // R
-                visc(ip - 2, jp, 2);       // P, low
-                visc(ip - 2, jp - 1, 2);   // P, high
-                visc(ip, jp, 3);           // M, low
-                visc(ip, jp - 1, 3);       // M, high
+                const int is[6] = {ip - 1, ip - 1, ip - 2, ip - 2, ip, ip};
+                const int gs[6] = {jp, jp - 1, jp, jp - 1, jp, jp - 1};
+                const int roles[6] = {0, 1, 2, 2, 3, 3};
+#pragma unroll
+                for (int t = 0; t < 6; t++) {
+                    const double* r = rec(is[t], gs[t]);
+                    if (r) visc(r, c.geo_j + ((size_t)is[t] * c.nj + gs[t]) * NGEO, roles[t]);
+                }
             }
         }
+        const bool phys = ip >= 1 && ip <= c.nic && jp >= 1 && jp <= c.njc;
         if (NQ == 5 && phys && c.viscous) {
             const double* s = srec + ((size_t)(ip - 1) * c.njc + (jp - 1)) * SRW;
             acc[P_RHO] += s[S_RHO]; acc[P_NUT] += s[S_NUT]; acc[P_MU] += s[S_MU];

@@ -283,7 +283,7 @@ int alloc(T** p, size_t n) {
 // forward pipelines
 // ---------------------------------------------------------------------------
 template <class T, int NQ>
-int launch_forward(st_ctx* x, const DevCase& dc, const T* q, const T* beta, T* P, T* phi_i, T* phi_j, T* Fi, T* Fj,
+int launch_forward(st_ctx* x, const DevCase& dc, const T* q, const T* beta, T* P, T* lim, T* Fi, T* Fj,
                    T* Gi, T* Gj, T* rhs, int order) {
     cudaStream_t s = x->stream;
     const unsigned gc = grid_for(x->ncell);
@@ -292,16 +292,16 @@ int launch_forward(st_ctx* x, const DevCase& dc, const T* q, const T* beta, T* P
     k_bc<T, NQ><<<1, 1024, 0, s>>>(dc, P);
     stx::mark(x, "k_bc");
     if (order == 2) {
-        k_limiter<T, NQ><<<gc, 256, 0, s>>>(dc, P, phi_i, phi_j);
+        k_limiter<T, NQ, false><<<gc, 256, 0, s>>>(dc, P, lim);
         stx::mark(x, "k_limiter");
-        k_face<T, NQ, 0, 2><<<grid_for(x->nfi), 256, 0, s>>>(dc, P, phi_i, Fi, Gi);
+        k_face<T, NQ, 0, 2><<<grid_for(x->nfi), 256, 0, s>>>(dc, P, lim, Fi, Gi);
         stx::mark(x, "k_face_i");
-        k_face<T, NQ, 1, 2><<<grid_for(x->nfj), 256, 0, s>>>(dc, P, phi_j, Fj, Gj);
+        k_face<T, NQ, 1, 2><<<grid_for(x->nfj), 256, 0, s>>>(dc, P, lim, Fj, Gj);
         stx::mark(x, "k_face_j");
     } else {
-        k_face<T, NQ, 0, 1><<<grid_for(x->nfi), 256, 0, s>>>(dc, P, phi_i, Fi, Gi);
+        k_face<T, NQ, 0, 1><<<grid_for(x->nfi), 256, 0, s>>>(dc, P, lim, Fi, Gi);
         stx::mark(x, "k_face_i");
-        k_face<T, NQ, 1, 1><<<grid_for(x->nfj), 256, 0, s>>>(dc, P, phi_j, Fj, Gj);
+        k_face<T, NQ, 1, 1><<<grid_for(x->nfj), 256, 0, s>>>(dc, P, lim, Fj, Gj);
         stx::mark(x, "k_face_j");
     }
     k_cell<T, NQ><<<gc, 256, 0, s>>>(dc, P, Fi, Fj, Gi, Gj, beta, rhs);
@@ -317,8 +317,8 @@ int order_of(st_ctx* x, int lhs) { return lhs ? x->c.lhs_order : x->c.order; }
 namespace stx {
 int run_residual(st_ctx* x, const double* q, const double* beta, double* rhs, int order) {
     if (x->nq == 5)
-        return launch_forward<double, 5>(x, x->dc, q, beta, x->P, x->phi_i, x->phi_j, x->Fi, x->Fj, x->Gi, x->Gj, rhs, order);
-    return launch_forward<double, 4>(x, x->dc, q, beta, x->P, x->phi_i, x->phi_j, x->Fi, x->Fj, x->Gi, x->Gj, rhs, order);
+        return launch_forward<double, 5>(x, x->dc, q, beta, x->P, x->lim, x->Fi, x->Fj, x->Gi, x->Gj, rhs, order);
+    return launch_forward<double, 4>(x, x->dc, q, beta, x->P, x->lim, x->Fi, x->Fj, x->Gi, x->Gj, rhs, order);
 }
 }  // namespace stx
 
@@ -386,7 +386,7 @@ int st_create(const st_case* c, const double* xv, const double* yv, int device, 
     int rc = ST_OK;
 #define AL(p, n) if (rc == ST_OK) rc = alloc(&(p), (n))
     AL(x->q, x->ncell * nq); AL(x->rhs, x->ncell * nq); AL(x->beta, x->ncell); AL(x->P, x->npad * NP);
-    AL(x->phi_i, x->ncell * nq); AL(x->phi_j, x->ncell * nq); AL(x->Fi, x->nfi * nq); AL(x->Fj, x->nfj * nq);
+    AL(x->lim, x->ncell * 12 * 5); AL(x->Fi, x->nfi * nq); AL(x->Fj, x->nfj * nq);
     AL(x->Gi, x->nfi * 4); AL(x->Gj, x->nfj * 4); AL(x->vol_d, x->ncell); AL(x->ivol_d, x->ncell);
     AL(x->geo_i, x->nfi * NGEO); AL(x->geo_j, x->nfj * NGEO); AL(x->wd, x->ncell);
     AL(x->nchi_d, x->nchi.size()); AL(x->neta_d, x->neta.size()); AL(x->dsmin_d, x->ncell); AL(x->dt, x->ncell * nq);
@@ -465,12 +465,12 @@ int st_create(const st_case* c, const double* xv, const double* yv, int device, 
 int st_destroy(st_ctx* x) {
     if (!x) return ST_OK;
     if (x->stream) cudaStreamSynchronize(x->stream);
-    double* bufs[] = {x->q, x->rhs, x->beta, x->P, x->phi_i, x->phi_j, x->Fi, x->Fj, x->Gi, x->Gj, x->vol_d, x->ivol_d,
+    double* bufs[] = {x->q, x->rhs, x->beta, x->P, x->lim, x->Fi, x->Fj, x->Gi, x->Gj, x->vol_d, x->ivol_d,
                       x->geo_i, x->geo_j, x->wd, x->nchi_d, x->neta_d, x->dsmin_d, x->dt, x->norm_part, x->norm_out,
-                      x->cf, x->wall_dx_d, x->Pbar, x->w, x->srec, x->arec_i, x->arec_j, x->lrec, x->psi_tmp,
+                      x->cf, x->wall_dx_d, x->Pbar, x->srec, x->arec_i, x->arec_j, x->psi_tmp,
                       x->outq_tmp, x->outb_tmp, x->tape};
     for (double* b : bufs) if (b) cudaFree(b);
-    st::dual* dbufs[] = {x->qd, x->Pd, x->phid_i, x->phid_j, x->Fdi, x->Fdj, x->Gdi, x->Gdj, x->rhsd, x->betad};
+    st::dual* dbufs[] = {x->qd, x->Pd, x->limd, x->Fdi, x->Fdj, x->Gdi, x->Gdj, x->rhsd, x->betad};
     for (st::dual* b : dbufs) if (b) cudaFree(b);
     if (x->bcs_d) cudaFree(x->bcs_d);
     if (x->err_d) cudaFree(x->err_d);
@@ -595,8 +595,7 @@ int st_jvp_device(st_ctx* x, const double* v_dev, const double* vb_dev, double* 
         int rc = ST_OK;
         if (rc == ST_OK) rc = alloc(&x->qd, x->ncell * nq);
         if (rc == ST_OK) rc = alloc(&x->Pd, x->npad * NP);
-        if (rc == ST_OK) rc = alloc(&x->phid_i, x->ncell * nq);
-        if (rc == ST_OK) rc = alloc(&x->phid_j, x->ncell * nq);
+        if (rc == ST_OK) rc = alloc(&x->limd, x->ncell * 4 * 5);
         if (rc == ST_OK) rc = alloc(&x->Fdi, x->nfi * nq);
         if (rc == ST_OK) rc = alloc(&x->Fdj, x->nfj * nq);
         if (rc == ST_OK) rc = alloc(&x->Gdi, x->nfi * 4);
@@ -613,10 +612,10 @@ int st_jvp_device(st_ctx* x, const double* v_dev, const double* vb_dev, double* 
     k_to_dual<<<grid_for(x->ncell), 256, 0, s>>>(x->beta, vb_dev, x->betad, x->ncell, 1.0);
     int rc;
     if (nq == 5)
-        rc = launch_forward<st::dual, 5>(x, x->dc, x->qd, x->betad, x->Pd, x->phid_i, x->phid_j, x->Fdi, x->Fdj,
+        rc = launch_forward<st::dual, 5>(x, x->dc, x->qd, x->betad, x->Pd, x->limd, x->Fdi, x->Fdj,
                                           x->Gdi, x->Gdj, x->rhsd, order_of(x, lhs));
     else
-        rc = launch_forward<st::dual, 4>(x, x->dc, x->qd, x->betad, x->Pd, x->phid_i, x->phid_j, x->Fdi, x->Fdj,
+        rc = launch_forward<st::dual, 4>(x, x->dc, x->qd, x->betad, x->Pd, x->limd, x->Fdi, x->Fdj,
                                           x->Gdi, x->Gdj, x->rhsd, order_of(x, lhs));
     if (rc) return rc;
     k_tangent<<<grid_for(x->ncell * nq), 256, 0, s>>>(x->rhsd, jv_dev, x->ncell * nq);
@@ -660,7 +659,8 @@ int st_profile_pipeline(st_ctx* x, int which, int lhs, double* ms, int max_n, ch
     cudaEventRecord(x->prof_ev[0], x->stream);
     int rc;
     if (which == 0) rc = stx::run_residual(x, x->q, x->beta, x->rhs, order_of(x, lhs));
-    else rc = st_vjp_device(x, x->rhs, nullptr, nullptr, lhs);
+    else if (which == 1) rc = st_vjp_device(x, x->rhs, nullptr, nullptr, lhs);
+    else rc = st_residual_vjp_device(x, x->rhs, x->rhs, nullptr, nullptr, lhs);
     x->prof_on = false;
     if (rc) return rc;
     ST_CUDA(cudaEventSynchronize(x->prof_ev[x->prof_n]));

@@ -22,7 +22,7 @@ struct st_ctx {
 
     // device buffers (double path)
     double *q = nullptr, *rhs = nullptr, *beta = nullptr, *P = nullptr;
-    double *phi_i = nullptr, *phi_j = nullptr, *Fi = nullptr, *Fj = nullptr, *Gi = nullptr, *Gj = nullptr;
+    double *lim = nullptr, *Fi = nullptr, *Fj = nullptr, *Gi = nullptr, *Gj = nullptr;
     double *vol_d = nullptr, *ivol_d = nullptr, *geo_i = nullptr, *geo_j = nullptr, *wd = nullptr;
     double *nchi_d = nullptr, *neta_d = nullptr, *dsmin_d = nullptr, *dt = nullptr;
     double *norm_part = nullptr, *norm_out = nullptr, *cf = nullptr, *wall_dx_d = nullptr;
@@ -30,12 +30,12 @@ struct st_ctx {
     int* err_d = nullptr;
 
     // forward-mode (dual) buffers, allocated on the first JVP call
-    st::dual *qd = nullptr, *Pd = nullptr, *phid_i = nullptr, *phid_j = nullptr;
+    st::dual *qd = nullptr, *Pd = nullptr, *limd = nullptr;
     st::dual *Fdi = nullptr, *Fdj = nullptr, *Gdi = nullptr, *Gdj = nullptr, *rhsd = nullptr, *betad = nullptr;
 
     // adjoint buffers, allocated on the first VJP call
-    double *Pbar = nullptr, *w = nullptr, *srec = nullptr, *arec_i = nullptr, *arec_j = nullptr;
-    double *lrec = nullptr, *psi_tmp = nullptr, *outq_tmp = nullptr, *outb_tmp = nullptr, *tape = nullptr;
+    double *Pbar = nullptr, *srec = nullptr, *arec_i = nullptr, *arec_j = nullptr;
+    double *psi_tmp = nullptr, *outq_tmp = nullptr, *outb_tmp = nullptr, *tape = nullptr;
 
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     // per-launch profiling (st_profile_pipeline): an event after each launch

@@ -173,36 +173,53 @@ __global__ void __launch_bounds__(1024) k_bc(DevCase c, T* __restrict__ P) {
 }
 
 // ----------------------------------------------------------------------------
-// K3  MUSCL limiter factor per cell and direction,
-//     ReconstructionSecondOrder (src/model/reconstruction.cpp:85-113):
-//     phi = 0.25 (3 a b + eps) / (2 (b - a)^2 + 3 a b + eps)
+// K3  MUSCL slopes per cell and direction, ReconstructionSecondOrder
+//     (src/model/reconstruction.cpp:85-113): with d- = P(c)-P(c-1),
+//     d+ = P(c+1)-P(c) and the limiter
+//         phi = 0.25 (3 d+ d- + eps) / (2 (d+ - d-)^2 + 3 d+ d- + eps),
+//     the cell's high face sees P + sL, its low face P - sR, where
+//         sL = phi (THM d- + THP d+),  sR = phi (THP d- + THM d+).
+//     With ADJ the kernel also stores dsL/dd-, dsL/dd+, dsR/dd-, dsR/dd+ for
+//     the adjoint, from the same reciprocal.
+// lim layout: group-major [group][cell][5]; groups 0..3 = (sL,sR) of i then j,
+// groups 4..11 = (dsL/dd-, dsL/dd+, dsR/dd-, dsR/dd+) of i then j.
 // ----------------------------------------------------------------------------
-template <class T, int NQ>
-__global__ void __launch_bounds__(256) k_limiter(DevCase c, const T* __restrict__ P, T* __restrict__ phi_i,
-                                                 T* __restrict__ phi_j) {
+enum { LIM_SL = 0, LIM_SR = 1, LIM_AM = 2, LIM_AP = 3, LIM_BM = 4, LIM_BP = 5 };
+__host__ __device__ inline size_t lim_off(const DevCase& c, int dir, int g, size_t cell) {
+    const int grp = g < 2 ? dir * 2 + g : 4 + dir * 4 + (g - 2);
+    return ((size_t)grp * ((size_t)c.nic * c.njc) + cell) * 5;
+}
+
+template <class T, int NQ, bool ADJ>
+__global__ void __launch_bounds__(256) k_limiter(DevCase c, const T* __restrict__ P, T* __restrict__ lim) {
     const size_t n = (size_t)c.nic * c.njc;
     const int slot[5] = {P_RHO, P_U, P_V, P_P, P_NUT};
     for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += (size_t)gridDim.x * blockDim.x) {
         const int i = (int)(idx / c.njc), j = (int)(idx % c.njc);
         const T* pc = P + pidx(c, i + 1, j + 1);
-        const T* pw = P + pidx(c, i, j + 1);
-        const T* pe = P + pidx(c, i + 2, j + 1);
-        const T* ps = P + pidx(c, i + 1, j);
-        const T* pn = P + pidx(c, i + 1, j + 2);
 #pragma unroll
-        for (int k = 0; k < NQ; k++) {
-            const int m = slot[k];
-            {
-                T fa = pc[m] - pw[m], fb = pe[m] - pc[m];
-                T a1 = 3.0 * fb * fa;
-                T a2 = 2.0 * (fb - fa) * (fb - fa) + a1;
-                phi_i[idx * NQ + k] = 0.25 * (a1 + c.eps_chi) * rcp(a2 + c.eps_chi);
-            }
-            {
-                T fa = pc[m] - ps[m], fb = pn[m] - pc[m];
-                T a1 = 3.0 * fb * fa;
-                T a2 = 2.0 * (fb - fa) * (fb - fa) + a1;
-                phi_j[idx * NQ + k] = 0.25 * (a1 + c.eps_eta) * rcp(a2 + c.eps_eta);
+        for (int dir = 0; dir < 2; dir++) {
+            const T* pm = dir == 0 ? P + pidx(c, i, j + 1) : P + pidx(c, i + 1, j);
+            const T* pp = dir == 0 ? P + pidx(c, i + 2, j + 1) : P + pidx(c, i + 1, j + 2);
+            const double eps = dir == 0 ? c.eps_chi : c.eps_eta;
+#pragma unroll
+            for (int k = 0; k < NQ; k++) {
+                const int m = slot[k];
+                const T fa = pc[m] - pm[m], fb = pp[m] - pc[m];
+                const T a1 = 3.0 * fb * fa;
+                const T inv = rcp(2.0 * (fb - fa) * (fb - fa) + a1 + eps);
+                const T ph = 0.25 * (a1 + eps) * inv;
+                const T tl = THM * fa + THP * fb, tr = THP * fa + THM * fb;
+                lim[lim_off(c, dir, LIM_SL, idx) + k] = ph * tl;
+                lim[lim_off(c, dir, LIM_SR, idx) + k] = ph * tr;
+                if (ADJ) {
+                    const T dfa = (0.75 * fb - ph * (3.0 * fb - 4.0 * (fb - fa))) * inv;
+                    const T dfb = (0.75 * fa - ph * (3.0 * fa + 4.0 * (fb - fa))) * inv;
+                    lim[lim_off(c, dir, LIM_AM, idx) + k] = ph * THM + tl * dfa;
+                    lim[lim_off(c, dir, LIM_AP, idx) + k] = ph * THP + tl * dfb;
+                    lim[lim_off(c, dir, LIM_BM, idx) + k] = ph * THP + tr * dfa;
+                    lim[lim_off(c, dir, LIM_BP, idx) + k] = ph * THM + tr * dfb;
+                }
             }
         }
     }
@@ -314,7 +331,7 @@ __device__ inline FaceIdx face_idx(const DevCase& c, int a, int b) {
 //     the cell source needs.
 // ----------------------------------------------------------------------------
 template <class T, int NQ, int DIR, int ORDER>
-__global__ void __launch_bounds__(256) k_face(DevCase c, const T* __restrict__ P, const T* __restrict__ phi,
+__global__ void __launch_bounds__(256) k_face(DevCase c, const T* __restrict__ P, const T* __restrict__ lim,
                                               T* __restrict__ F, T* __restrict__ G) {
     const int na = DIR == 0 ? c.ni : c.nic;
     const int nb = DIR == 0 ? c.njc : c.nj;
@@ -334,15 +351,8 @@ __global__ void __launch_bounds__(256) k_face(DevCase c, const T* __restrict__ P
             qL[k] = pL[m];
             qR[k] = pR[m];
             if (ORDER == 2) {
-                const T dC = pR[m] - pL[m];
-                if (fi.limL) {
-                    const T dL = pL[m] - P[fi.LL + m];
-                    qL[k] = qL[k] + phi[fi.phL * NQ + k] * (THM * dL + THP * dC);
-                }
-                if (fi.limR) {
-                    const T dR = P[fi.RR + m] - pR[m];
-                    qR[k] = qR[k] - phi[fi.phR * NQ + k] * (THP * dC + THM * dR);
-                }
+                if (fi.limL) qL[k] = qL[k] + lim[lim_off(c, DIR, LIM_SL, fi.phL) + k];
+                if (fi.limR) qR[k] = qR[k] - lim[lim_off(c, DIR, LIM_SR, fi.phR) + k];
             }
         }
         T f[NQ];

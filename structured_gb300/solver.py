@@ -67,6 +67,9 @@ def load_library() -> ctypes.CDLL:
         "st_jvp_device": (I, [V, V, V, V, I]),
         "st_vjp_device": (I, [V, V, V, V, I]),
         "st_vjp": (I, [V, _P, _P, _P, I]),
+        "st_residual_vjp_device": (I, [V, V, V, V, V, I]),
+        "st_residual_vjp": (I, [V, _P, _P, _P, _P, I]),
+        "st_fused_launch_count": (I, [V, I]),
         "st_probe_fp64": (I, [V, ctypes.POINTER(D)]),
         "st_last_kernel_ms": (I, [V, ctypes.POINTER(D), ctypes.POINTER(D)]),
         "st_profile_pipeline": (I, [V, I, I, _P, I, ctypes.c_char_p, I, ctypes.POINTER(I)]),
@@ -189,6 +192,26 @@ class EulerEquation:
         _check(self.lib.st_vjp(self.h, _ptr(psi), _ptr(oq), _ptr(ob), int(lhs)), "st_vjp")
         return oq, ob
 
+    def residual_vjp_device(self, psi_ptr: int, rhs_ptr: int, outq_ptr: int | None, outb_ptr: int | None,
+                            lhs: bool = False) -> None:
+        """Residual and adjoint of the context state in one sweep."""
+        _check(self.lib.st_residual_vjp_device(self.h, _vp(psi_ptr), _vp(rhs_ptr), _vp(outq_ptr), _vp(outb_ptr),
+                                               int(lhs)), "st_residual_vjp_device")
+
+    def residual_vjp(self, psi: np.ndarray, lhs: bool = False):
+        psi = np.ascontiguousarray(psi, dtype=np.float64)
+        rhs = np.empty(self.shape)
+        oq = np.empty(self.shape)
+        ob = np.empty((self.nic, self.njc))
+        _check(self.lib.st_residual_vjp(self.h, _ptr(psi), _ptr(rhs), _ptr(oq), _ptr(ob), int(lhs)), "st_residual_vjp")
+        return rhs, oq, ob
+
+    def fused_launch_count(self, lhs: bool = False) -> int:
+        n = self.lib.st_fused_launch_count(self.h, int(lhs))
+        if n < 0:
+            _check(n, "st_fused_launch_count")
+        return n
+
     def device_state(self):
         q, r, s = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
         _check(self.lib.st_device_state(self.h, ctypes.byref(q), ctypes.byref(r), ctypes.byref(s)), "st_device_state")
@@ -204,7 +227,8 @@ class EulerEquation:
         ms = np.zeros(32)
         buf = ctypes.create_string_buffer(1024)
         n = ctypes.c_int()
-        _check(self.lib.st_profile_pipeline(self.h, 0 if which == "residual" else 1, int(lhs), _ptr(ms), 32, buf,
+        code = {"residual": 0, "adjoint": 1, "fused": 2}[which]
+        _check(self.lib.st_profile_pipeline(self.h, code, int(lhs), _ptr(ms), 32, buf,
                                             1024, ctypes.byref(n)), "st_profile_pipeline")
         names = buf.value.decode().split(",")
         out = {}

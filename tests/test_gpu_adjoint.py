@@ -98,3 +98,23 @@ def test_vjp_is_deterministic(gpu_lib, tmp_path):
     a = eq.vjp(psi)
     b = eq.vjp(psi)
     assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
+@pytest.mark.parametrize("turb", ["none", "sa"])
+def test_fused_residual_adjoint_matches_separate_calls(gpu_lib, port_built, tmp_path, turb):
+    """st_residual_vjp (one sweep) gives the same residual as st_residual and
+    the same products as st_vjp."""
+    from oracle.port import PortCase
+    c = flat_plate(tmp_path, "fused", 67, 41, turbulence=turb)
+    xv, yv = C.load_grid(c)
+    q = C.perturbed_state(c, 46)
+    eq = eq_for(c, xv, yv)
+    psi = np.random.default_rng(47).standard_normal(q.shape)
+    rhs_a = eq.calc_residual(q)
+    oq_a, ob_a = eq.vjp(psi)
+    rhs_b, oq_b, ob_b = eq.residual_vjp(psi)
+    port = PortCase(c, xv, yv)
+    from helpers import rel_err
+    assert rel_err(rhs_b, rhs_a, port.flux_scale(q)) < 1e-13
+    assert rel_err(rhs_b, port.residual(q), port.flux_scale(q)) < 1e-12
+    assert np.array_equal(oq_a, oq_b) and np.array_equal(ob_a, ob_b)
