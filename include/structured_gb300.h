@@ -143,6 +143,20 @@ int st_fused_launch_count(st_ctx* ctx, int lhs);
 /* Kernel launches one st_residual_device / st_vjp_device call makes. */
 int st_launch_counts(st_ctx* ctx, int lhs, int* residual, int* vjp);
 
+/* L2 norm of each of the nq components of a residual that is already on the
+ * device (rhs_dev: [ncell][nq] doubles), written to out_dev[nq] on `stream`
+ * (a cudaStream_t; NULL = default stream); asynchronous.  This entry point
+ * has no counterpart in the reference.  It allocates no device memory, for
+ * callers that cannot allocate once running (an application that has reserved
+ * the device for its own pool, or a loop that cannot afford the device-wide
+ * synchronisation of cudaMalloc/cudaFree): its partial sums live in a fixed
+ * 64 KiB device array inside the library, held by every device that loads it
+ * until the process exits.  Limit: nq <= 8.  The first call on each device
+ * looks up that array's address (cudaGetSymbolAddress); make it outside any
+ * stream capture.  All calls share the array: calls that overlap on the GPU
+ * race. */
+int st_norms_noalloc(const double* rhs_dev, long long ncell, int nq, double* out_dev, void* stream);
+
 /* Diagnostics: dense FP64 FMA throughput of this device (TFLOP/s). */
 int st_probe_fp64(st_ctx* ctx, double* tflops);
 /* Runs one pipeline on the context state (which = 0: residual; 1: adjoint VJP
