@@ -76,6 +76,24 @@ typedef struct st_solve_stats {
     double residual0, residual;     /* initial / final linear residual 2-norms */
 } st_solve_stats;
 
+/* Pseudo-time Newton parameters: the [solver] keys of src/utils/config.cpp:
+ * 42-56 (cfl, ramps, tolerance, iteration_max) plus the Krylov settings. */
+typedef struct st_solve_params {
+    int32_t max_steps;                    /* iteration_max */
+    int32_t krylov_m;                     /* GMRES restart length */
+    int32_t krylov_maxit;                 /* GMRES iterations per pseudo-time step */
+    int32_t cfl_ramp, cfl_ramp_iteration;
+    int32_t under_relaxation_ramp, under_relaxation_ramp_iteration;
+    int32_t max_failures;                 /* divergence-guard restarts allowed */
+    double cfl, cfl_max, cfl_ramp_exponent;
+    double under_relaxation, under_relaxation_ramp_exponent;
+    double tolerance;                     /* stop when max_k ||R_k||_2 <= tolerance */
+    double rel_tolerance;                 /* ... or <= rel_tolerance * initial */
+    double krylov_rtol;
+    double ser_exponent;                  /* > 0: also CFL >= cfl (r0/r)^ser_exponent */
+    double divergence_factor;             /* residual growth over the best seen that counts as divergence */
+} st_solve_params;
+
 const char* st_last_error(void);
 int st_version(void);
 
@@ -139,6 +157,38 @@ int st_residual_vjp(st_ctx* ctx, const double* psi_host, double* rhs_host, doubl
                     double* out_beta_host, int lhs);
 /* Kernel launches one st_residual_vjp_device call makes. */
 int st_fused_launch_count(st_ctx* ctx, int lhs);
+
+/* Block Jacobian dR/dQ of the residual (lhs != 0: lhs_order) at the context
+ * state, 13-point stencil of nq x nq blocks, from exact forward-mode JVPs over
+ * a 5x5 cell colouring.  Replaces ADOL-C's sparse_jac and the COO buffers of
+ * src/solver/solver.cpp:156-171.  Not available with periodic or wake BCs. */
+int st_jacobian_assemble(st_ctx* ctx, int lhs);
+/* Copy of the blocks, [nic][njc][13][nq][nq] (row component major); offsets
+ * (di,dj): (0,0),(-1,0),(1,0),(0,-1),(0,1),(-2,0),(2,0),(0,-2),(0,2),
+ * (-1,-1),(-1,1),(1,-1),(1,1). */
+int st_jacobian_blocks(st_ctx* ctx, double* blocks_host);
+/* out = J v (transpose != 0: J^T v) with the assembled blocks. */
+int st_jacobian_apply_device(st_ctx* ctx, const double* v_dev, double* out_dev, int transpose);
+/* One linear solve of the implicit step, (I/dt(cfl) - J) x = b (or its
+ * transpose): the set_lhs / set_rhs / solve of the reference's linear-solver
+ * classes (src/linearsolver/ls_eigen.cpp:23-71), here restarted GMRES with a
+ * block-tridiagonal j-line preconditioner; x holds the initial guess. */
+int st_linear_solve_device(st_ctx* ctx, double cfl, const double* b_dev, double* x_dev, int transpose,
+                           int krylov_m, int maxit, double rtol, st_solve_stats* stats);
+/* Pseudo-time Newton to steady state on the context state: Solver::solve /
+ * Solver::step (src/solver/solver.cpp:53-236) with the implicit (ADOL-C) path.
+ * history (may be NULL) receives per step [step, cfl, krylov iterations,
+ * ||R_0..nq-1||_2]; *steps_done the steps taken.  Returns ST_ERR_NOCONV if the
+ * tolerance is not reached in max_steps. */
+int st_solve(st_ctx* ctx, const st_solve_params* params, st_solve_stats* stats, double* history,
+             int history_len, int* steps_done);
+/* grad_dev = d(sum_i w_i Cf_i)/dQ at the context state for wall weights
+ * w_host[nic] (drag: w = dx; inversion misfit: w = 2 (Cf - Cf*)). */
+int st_cf_gradient_device(st_ctx* ctx, const double* w_host, double* grad_dev);
+/* Adjoint solve (dR/dQ)^T psi = b with the exact Jacobian of the residual;
+ * the preconditioner adds I/dt(cfl_prec).  psi holds the initial guess. */
+int st_adjoint_solve_device(st_ctx* ctx, const double* b_dev, double* psi_dev, double cfl_prec, int krylov_m,
+                            int maxit, double rtol, st_solve_stats* stats);
 
 /* Kernel launches one st_residual_device / st_vjp_device call makes. */
 int st_launch_counts(st_ctx* ctx, int lhs, int* residual, int* vjp);

@@ -66,3 +66,14 @@ def make_case_struct(c: "_case.Case"):
     s.plate_x_end = c.plate_x_end
     s.bcs = ctypes.cast(bcs, ctypes.POINTER(StBc))
     return s, bcs
+
+
+class StSolveParams(ctypes.Structure):
+    _fields_ = [("max_steps", ctypes.c_int32), ("krylov_m", ctypes.c_int32), ("krylov_maxit", ctypes.c_int32),
+                ("cfl_ramp", ctypes.c_int32), ("cfl_ramp_iteration", ctypes.c_int32),
+                ("under_relaxation_ramp", ctypes.c_int32), ("under_relaxation_ramp_iteration", ctypes.c_int32),
+                ("max_failures", ctypes.c_int32),
+                ("cfl", ctypes.c_double), ("cfl_max", ctypes.c_double), ("cfl_ramp_exponent", ctypes.c_double),
+                ("under_relaxation", ctypes.c_double), ("under_relaxation_ramp_exponent", ctypes.c_double),
+                ("tolerance", ctypes.c_double), ("rel_tolerance", ctypes.c_double), ("krylov_rtol", ctypes.c_double),
+                ("ser_exponent", ctypes.c_double), ("divergence_factor", ctypes.c_double)]

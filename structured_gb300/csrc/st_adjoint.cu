@@ -98,6 +98,10 @@ int run_fused(st_ctx* x, const double* psi, double* rhs, double* outq, double* o
 
 }  // namespace
 
+namespace stx {
+int ensure_adjoint_buffers(st_ctx* x) { return ensure(x); }
+}  // namespace stx
+
 extern "C" {
 
 int st_vjp_device(st_ctx* x, const double* psi, double* outq, double* outb, int lhs) {

@@ -293,7 +293,7 @@ __global__ void __launch_bounds__(256) k_face_grad(DevCase c, const double* __re
 // so the source adjoint is psi_4 (V/V).  Writes the source value, the
 // adjoints of the cell's own rho, nut, mu, and of the four face gradient parts
 // it averages (the same for all four faces), and (dR/dbeta)^T psi.
-__global__ void __launch_bounds__(256) k_cell_src(DevCase c, const double* __restrict__ P, const double* __restrict__ Gi,
+static __global__ void __launch_bounds__(256) k_cell_src(DevCase c, const double* __restrict__ P, const double* __restrict__ Gi,
                                                   const double* __restrict__ Gj, const double* __restrict__ beta,
                                                   const double* __restrict__ psi, double* __restrict__ srec,
                                                   double* __restrict__ outb) {

@@ -315,6 +315,63 @@ int order_of(st_ctx* x, int lhs) { return lhs ? x->c.lhs_order : x->c.order; }
 }  // namespace
 
 namespace stx {
+int run_jvp(st_ctx* x, const double* v_dev, const double* vb_dev, double* jv_dev, int order) {
+    const int nq = x->nq;
+    if (!x->qd) {
+        int rc = ST_OK;
+        if (rc == ST_OK) rc = alloc(&x->qd, x->ncell * nq);
+        if (rc == ST_OK) rc = alloc(&x->Pd, x->npad * NP);
+        if (rc == ST_OK) rc = alloc(&x->limd, x->ncell * 4 * 5);
+        if (rc == ST_OK) rc = alloc(&x->Fdi, x->nfi * nq);
+        if (rc == ST_OK) rc = alloc(&x->Fdj, x->nfj * nq);
+        if (rc == ST_OK) rc = alloc(&x->Gdi, x->nfi * 4);
+        if (rc == ST_OK) rc = alloc(&x->Gdj, x->nfj * 4);
+        if (rc == ST_OK) rc = alloc(&x->rhsd, x->ncell * nq);
+        if (rc == ST_OK) rc = alloc(&x->betad, x->ncell);
+        if (rc) return rc;
+        ST_CUDA(cudaMemsetAsync(x->Pd, 0, x->npad * NP * sizeof(st::dual), x->stream));
+        ST_CUDA(cudaMemsetAsync(x->Gdi, 0, x->nfi * 4 * sizeof(st::dual), x->stream));
+        ST_CUDA(cudaMemsetAsync(x->Gdj, 0, x->nfj * 4 * sizeof(st::dual), x->stream));
+    }
+    cudaStream_t s = x->stream;
+    k_to_dual<<<grid_for(x->ncell * nq), 256, 0, s>>>(x->q, v_dev, x->qd, x->ncell * nq, 0.0);
+    k_to_dual<<<grid_for(x->ncell), 256, 0, s>>>(x->beta, vb_dev, x->betad, x->ncell, 1.0);
+    int rc;
+    if (nq == 5)
+        rc = launch_forward<st::dual, 5>(x, x->dc, x->qd, x->betad, x->Pd, x->limd, x->Fdi, x->Fdj,
+                                          x->Gdi, x->Gdj, x->rhsd, order);
+    else
+        rc = launch_forward<st::dual, 4>(x, x->dc, x->qd, x->betad, x->Pd, x->limd, x->Fdi, x->Fdj,
+                                          x->Gdi, x->Gdj, x->rhsd, order);
+    if (rc) return rc;
+    k_tangent<<<grid_for(x->ncell * nq), 256, 0, s>>>(x->rhsd, jv_dev, x->ncell * nq);
+    ST_LAUNCH_CHECK("jvp");
+    return ST_OK;
+}
+
+int run_dt(st_ctx* x, double cfl) {
+    if (x->nq == 5) k_dt<5><<<grid_for(x->ncell), 256, 0, x->stream>>>(x->dc, x->q, x->dsmin_d, cfl, x->dt);
+    else k_dt<4><<<grid_for(x->ncell), 256, 0, x->stream>>>(x->dc, x->q, x->dsmin_d, cfl, x->dt);
+    ST_LAUNCH_CHECK("k_dt");
+    return ST_OK;
+}
+
+int run_norms(st_ctx* x, const double* rhs, double* out) {
+    if (x->nq == 5) {
+        k_norm_partial<5><<<NORM_BLOCKS, 256, 0, x->stream>>>(rhs, x->ncell, x->norm_part);
+        k_norm_final<5><<<1, 32, 0, x->stream>>>(x->norm_part, NORM_BLOCKS, x->norm_out);
+    } else {
+        k_norm_partial<4><<<NORM_BLOCKS, 256, 0, x->stream>>>(rhs, x->ncell, x->norm_part);
+        k_norm_final<4><<<1, 32, 0, x->stream>>>(x->norm_part, NORM_BLOCKS, x->norm_out);
+    }
+    ST_LAUNCH_CHECK("norms");
+    ST_CUDA(cudaMemcpyAsync(out, x->norm_out, x->nq * 8, cudaMemcpyDeviceToHost, x->stream));
+    ST_CUDA(cudaStreamSynchronize(x->stream));
+    for (int k = 0; k < x->nq; k++)
+        if (!std::isfinite(out[k])) return fail(ST_ERR_NONFINITE, "non-finite residual norm");
+    return ST_OK;
+}
+
 int run_residual(st_ctx* x, const double* q, const double* beta, double* rhs, int order) {
     if (x->nq == 5)
         return launch_forward<double, 5>(x, x->dc, q, beta, x->P, x->lim, x->Fi, x->Fj, x->Gi, x->Gj, rhs, order);
@@ -468,7 +525,7 @@ int st_destroy(st_ctx* x) {
     double* bufs[] = {x->q, x->rhs, x->beta, x->P, x->lim, x->Fi, x->Fj, x->Gi, x->Gj, x->vol_d, x->ivol_d,
                       x->geo_i, x->geo_j, x->wd, x->nchi_d, x->neta_d, x->dsmin_d, x->dt, x->norm_part, x->norm_out,
                       x->cf, x->wall_dx_d, x->Pbar, x->srec, x->arec_i, x->arec_j, x->psi_tmp,
-                      x->outq_tmp, x->outb_tmp, x->tape};
+                      x->outq_tmp, x->outb_tmp, x->tape, x->jac, x->lfac, x->kv, x->kz, x->kw, x->kr, x->kh, x->kpart, x->dq, x->qsave};
     for (double* b : bufs) if (b) cudaFree(b);
     st::dual* dbufs[] = {x->qd, x->Pd, x->limd, x->Fdi, x->Fdj, x->Gdi, x->Gdj, x->rhsd, x->betad};
     for (st::dual* b : dbufs) if (b) cudaFree(b);
@@ -590,37 +647,9 @@ int st_skin_friction(st_ctx* x, double* cf_host, double* J) {
 
 int st_jvp_device(st_ctx* x, const double* v_dev, const double* vb_dev, double* jv_dev, int lhs) {
     if (!x || !v_dev || !jv_dev) return fail(ST_ERR_ARG, "st_jvp_device: null argument");
-    const int nq = x->nq;
-    if (!x->qd) {
-        int rc = ST_OK;
-        if (rc == ST_OK) rc = alloc(&x->qd, x->ncell * nq);
-        if (rc == ST_OK) rc = alloc(&x->Pd, x->npad * NP);
-        if (rc == ST_OK) rc = alloc(&x->limd, x->ncell * 4 * 5);
-        if (rc == ST_OK) rc = alloc(&x->Fdi, x->nfi * nq);
-        if (rc == ST_OK) rc = alloc(&x->Fdj, x->nfj * nq);
-        if (rc == ST_OK) rc = alloc(&x->Gdi, x->nfi * 4);
-        if (rc == ST_OK) rc = alloc(&x->Gdj, x->nfj * 4);
-        if (rc == ST_OK) rc = alloc(&x->rhsd, x->ncell * nq);
-        if (rc == ST_OK) rc = alloc(&x->betad, x->ncell);
-        if (rc) return rc;
-        ST_CUDA(cudaMemsetAsync(x->Pd, 0, x->npad * NP * sizeof(st::dual), x->stream));
-        ST_CUDA(cudaMemsetAsync(x->Gdi, 0, x->nfi * 4 * sizeof(st::dual), x->stream));
-        ST_CUDA(cudaMemsetAsync(x->Gdj, 0, x->nfj * 4 * sizeof(st::dual), x->stream));
-    }
-    cudaStream_t s = x->stream;
-    k_to_dual<<<grid_for(x->ncell * nq), 256, 0, s>>>(x->q, v_dev, x->qd, x->ncell * nq, 0.0);
-    k_to_dual<<<grid_for(x->ncell), 256, 0, s>>>(x->beta, vb_dev, x->betad, x->ncell, 1.0);
-    int rc;
-    if (nq == 5)
-        rc = launch_forward<st::dual, 5>(x, x->dc, x->qd, x->betad, x->Pd, x->limd, x->Fdi, x->Fdj,
-                                          x->Gdi, x->Gdj, x->rhsd, order_of(x, lhs));
-    else
-        rc = launch_forward<st::dual, 4>(x, x->dc, x->qd, x->betad, x->Pd, x->limd, x->Fdi, x->Fdj,
-                                          x->Gdi, x->Gdj, x->rhsd, order_of(x, lhs));
+    int rc = stx::run_jvp(x, v_dev, vb_dev, jv_dev, order_of(x, lhs));
     if (rc) return rc;
-    k_tangent<<<grid_for(x->ncell * nq), 256, 0, s>>>(x->rhsd, jv_dev, x->ncell * nq);
-    ST_LAUNCH_CHECK("jvp");
-    ST_CUDA(cudaStreamSynchronize(s));
+    ST_CUDA(cudaStreamSynchronize(x->stream));
     return ST_OK;
 }
 

@@ -35,6 +35,10 @@ struct st_ctx {
 
     // adjoint buffers, allocated on the first VJP call
     double *Pbar = nullptr, *srec = nullptr, *arec_i = nullptr, *arec_j = nullptr;
+    // implicit solver (allocated on first use)
+    double *jac = nullptr, *lfac = nullptr, *kv = nullptr, *kz = nullptr, *kw = nullptr, *kr = nullptr;
+    double *kh = nullptr, *kpart = nullptr, *dq = nullptr, *qsave = nullptr;
+    int kv_m = 0;
     double *psi_tmp = nullptr, *outq_tmp = nullptr, *outb_tmp = nullptr, *tape = nullptr;
 
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -76,5 +80,11 @@ inline void mark(st_ctx* x, const char* name) {
 }
 // forward pipeline on (q -> rhs) for the double path; beta may be null
 int run_residual(st_ctx* ctx, const double* q, const double* beta, double* rhs, int order);
+// forward-mode JVP of the order-`order` residual at the context state (async)
+int run_jvp(st_ctx* ctx, const double* v_dev, const double* vb_dev, double* jv_dev, int order);
+// time step into ctx->dt (async)
+int run_dt(st_ctx* ctx, double cfl);
+// L2 norms of rhs into host out[nq] (synchronises)
+int run_norms(st_ctx* ctx, const double* rhs, double* out);
 int ensure_adjoint_buffers(st_ctx* ctx);
 }  // namespace stx

@@ -75,6 +75,14 @@ def load_library() -> ctypes.CDLL:
         "st_profile_pipeline": (I, [V, I, I, _P, I, ctypes.c_char_p, I, ctypes.POINTER(I)]),
         "st_launch_counts": (I, [V, I, ctypes.POINTER(I), ctypes.POINTER(I)]),
         "st_device_state": (I, [V, ctypes.POINTER(V), ctypes.POINTER(V), ctypes.POINTER(V)]),
+        "st_jacobian_assemble": (I, [V, I]),
+        "st_jacobian_blocks": (I, [V, _P]),
+        "st_jacobian_apply_device": (I, [V, V, V, I]),
+        "st_linear_solve_device": (I, [V, D, V, V, I, I, I, D, ctypes.POINTER(abi.StSolveStats)]),
+        "st_solve": (I, [V, ctypes.POINTER(abi.StSolveParams), ctypes.POINTER(abi.StSolveStats), _P, I,
+                         ctypes.POINTER(I)]),
+        "st_cf_gradient_device": (I, [V, _P, V]),
+        "st_adjoint_solve_device": (I, [V, V, V, D, I, I, D, ctypes.POINTER(abi.StSolveStats)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -245,3 +253,93 @@ class EulerEquation:
         a, b = ctypes.c_double(), ctypes.c_double()
         _check(self.lib.st_last_kernel_ms(self.h, ctypes.byref(a), ctypes.byref(b)), "st_last_kernel_ms")
         return a.value, b.value
+
+
+def solve_params(case: C.Case | None = None, **over) -> abi.StSolveParams:
+    """Pseudo-time Newton parameters from a case's [solver] keys
+    (src/utils/config.cpp:42-56) with keyword overrides."""
+    p = abi.StSolveParams()
+    p.max_steps = case.iteration_max if case else 100
+    p.krylov_m, p.krylov_maxit, p.krylov_rtol = 40, 120, 1e-3
+    p.cfl = case.cfl if case else 10.0
+    p.cfl_max = 1e12
+    p.cfl_ramp = int(case.cfl_ramp) if case else 1
+    p.cfl_ramp_iteration = case.cfl_ramp_iteration if case else 5
+    p.cfl_ramp_exponent = case.cfl_ramp_exponent if case else 1.2
+    p.under_relaxation = case.under_relaxation if case else 1.0
+    p.under_relaxation_ramp = int(case.under_relaxation_ramp) if case else 0
+    p.under_relaxation_ramp_iteration = case.under_relaxation_ramp_iteration if case else 20
+    p.under_relaxation_ramp_exponent = case.under_relaxation_ramp_exponent if case else 1.1
+    p.tolerance = case.tolerance if case else 0.0
+    p.rel_tolerance = 0.0
+    p.ser_exponent = 0.0
+    p.divergence_factor = 1e4
+    p.max_failures = 5
+    for k, v in over.items():
+        setattr(p, k, v)
+    return p
+
+
+class Solver:
+    """Pseudo-time Newton driver on the GPU (reference: Solver::solve,
+    src/solver/solver.cpp:198-236, implicit path of Solver::step :53-196)."""
+
+    def __init__(self, eq: EulerEquation, **params):
+        self.eq = eq
+        self.params = solve_params(eq.case, **params)
+
+    def solve(self, raise_on_noconv: bool = True):
+        eq = self.eq
+        nq = eq.nq
+        stride = 3 + nq
+        hist = np.zeros(stride * (self.params.max_steps + 2))
+        st = abi.StSolveStats()
+        steps = ctypes.c_int()
+        rc = eq.lib.st_solve(eq.h, ctypes.byref(self.params), ctypes.byref(st), _ptr(hist), hist.size,
+                             ctypes.byref(steps))
+        rows = []
+        for k in range(0, hist.size, stride):
+            if k > 0 and hist[k] == 0 and hist[k + 1] == 0:
+                break
+            rows.append(hist[k:k + stride].copy())
+        history = np.array(rows)
+        if rc != abi.ST_OK and (raise_on_noconv or rc != -4):
+            _check(rc, "st_solve")
+        return rc == abi.ST_OK, history
+
+
+def _eq_extras():
+    def jacobian_assemble(self, lhs: bool = False):
+        _check(self.lib.st_jacobian_assemble(self.h, int(lhs)), "st_jacobian_assemble")
+
+    def jacobian_blocks(self):
+        b = np.empty((self.nic, self.njc, 13, self.nq, self.nq))
+        _check(self.lib.st_jacobian_blocks(self.h, _ptr(b)), "st_jacobian_blocks")
+        return b
+
+    def jacobian_apply_device(self, v_ptr, out_ptr, transpose=False):
+        _check(self.lib.st_jacobian_apply_device(self.h, _vp(v_ptr), _vp(out_ptr), int(transpose)),
+               "st_jacobian_apply_device")
+
+    def linear_solve_device(self, cfl, b_ptr, x_ptr, transpose=False, m=40, maxit=200, rtol=1e-8):
+        st = abi.StSolveStats()
+        _check(self.lib.st_linear_solve_device(self.h, float(cfl), _vp(b_ptr), _vp(x_ptr), int(transpose), m, maxit,
+                                               float(rtol), ctypes.byref(st)), "st_linear_solve_device")
+        return st
+
+    def cf_gradient_device(self, w: np.ndarray, grad_ptr):
+        w = np.ascontiguousarray(w, dtype=np.float64)
+        _check(self.lib.st_cf_gradient_device(self.h, _ptr(w), _vp(grad_ptr)), "st_cf_gradient_device")
+
+    def adjoint_solve_device(self, b_ptr, psi_ptr, cfl_prec=1e6, m=60, maxit=600, rtol=1e-10):
+        st = abi.StSolveStats()
+        _check(self.lib.st_adjoint_solve_device(self.h, _vp(b_ptr), _vp(psi_ptr), float(cfl_prec), m, maxit,
+                                                float(rtol), ctypes.byref(st)), "st_adjoint_solve_device")
+        return st
+
+    for f in (jacobian_assemble, jacobian_blocks, jacobian_apply_device, linear_solve_device, cf_gradient_device,
+              adjoint_solve_device):
+        setattr(EulerEquation, f.__name__, f)
+
+
+_eq_extras()
