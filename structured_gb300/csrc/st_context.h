@@ -36,9 +36,11 @@ struct st_ctx {
     // adjoint buffers, allocated on the first VJP call
     double *Pbar = nullptr, *srec = nullptr, *arec_i = nullptr, *arec_j = nullptr;
     // implicit solver (allocated on first use)
-    double *jac = nullptr, *lfac = nullptr, *kv = nullptr, *kz = nullptr, *kw = nullptr, *kr = nullptr;
+    double *jac = nullptr, *jac1 = nullptr, *lfac = nullptr, *kv = nullptr, *kz = nullptr, *kw = nullptr, *kr = nullptr;
     double *kh = nullptr, *kpart = nullptr, *dq = nullptr, *qsave = nullptr;
     int kv_m = 0;
+    bool jac1_is_jac = false;
+    unsigned* bar_d = nullptr;
     double *psi_tmp = nullptr, *outq_tmp = nullptr, *outb_tmp = nullptr, *tape = nullptr;
 
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
