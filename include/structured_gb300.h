@@ -85,6 +85,7 @@ typedef struct st_solve_params {
     int32_t cfl_ramp, cfl_ramp_iteration;
     int32_t under_relaxation_ramp, under_relaxation_ramp_iteration;
     int32_t max_failures;                 /* divergence-guard restarts allowed */
+    int32_t min_steps;                    /* Newton steps taken before the tolerance is checked */
     double cfl, cfl_max, cfl_ramp_exponent;
     double under_relaxation, under_relaxation_ramp_exponent;
     double tolerance;                     /* stop when max_k ||R_k||_2 <= tolerance */

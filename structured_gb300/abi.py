@@ -72,7 +72,7 @@ class StSolveParams(ctypes.Structure):
     _fields_ = [("max_steps", ctypes.c_int32), ("krylov_m", ctypes.c_int32), ("krylov_maxit", ctypes.c_int32),
                 ("cfl_ramp", ctypes.c_int32), ("cfl_ramp_iteration", ctypes.c_int32),
                 ("under_relaxation_ramp", ctypes.c_int32), ("under_relaxation_ramp_iteration", ctypes.c_int32),
-                ("max_failures", ctypes.c_int32),
+                ("max_failures", ctypes.c_int32), ("min_steps", ctypes.c_int32),
                 ("cfl", ctypes.c_double), ("cfl_max", ctypes.c_double), ("cfl_ramp_exponent", ctypes.c_double),
                 ("under_relaxation", ctypes.c_double), ("under_relaxation_ramp_exponent", ctypes.c_double),
                 ("tolerance", ctypes.c_double), ("rel_tolerance", ctypes.c_double), ("krylov_rtol", ctypes.c_double),

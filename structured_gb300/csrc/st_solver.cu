@@ -792,7 +792,7 @@ int st_solve(st_ctx* x, const st_solve_params* p, st_solve_stats* stats, double*
             history[hist++] = ls.iterations;
             for (int k = 0; k < nq; k++) history[hist++] = nrm[k];
         }
-        if (rn <= p->tolerance || rn <= p->rel_tolerance * r0) { converged = true; break; }
+        if (step >= p->min_steps && (rn <= p->tolerance || rn <= p->rel_tolerance * r0)) { converged = true; break; }
         if (step == p->max_steps) break;
         rc = stx::run_dt(x, cfl);
         if (rc) return rc;

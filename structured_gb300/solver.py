@@ -270,11 +270,14 @@ def solve_params(case: C.Case | None = None, **over) -> abi.StSolveParams:
     p.under_relaxation_ramp = int(case.under_relaxation_ramp) if case else 0
     p.under_relaxation_ramp_iteration = case.under_relaxation_ramp_iteration if case else 20
     p.under_relaxation_ramp_exponent = case.under_relaxation_ramp_exponent if case else 1.1
-    p.tolerance = case.tolerance if case else 0.0
+    # the reference's default tolerance (1e10, config.cpp:52) never mattered:
+    # its tolerance exit is disabled (solver.cpp:145); treat it as unset
+    p.tolerance = case.tolerance if (case and case.tolerance < 1e9) else 0.0
     p.rel_tolerance = 0.0
     p.ser_exponent = 0.0
     p.divergence_factor = 1e4
     p.max_failures = 5
+    p.min_steps = 0
     for k, v in over.items():
         setattr(p, k, v)
     return p
