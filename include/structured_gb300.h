@@ -191,6 +191,11 @@ int st_cf_gradient_device(st_ctx* ctx, const double* w_host, double* grad_dev);
 int st_adjoint_solve_device(st_ctx* ctx, const double* b_dev, double* psi_dev, double cfl_prec, int krylov_m,
                             int maxit, double rtol, st_solve_stats* stats);
 
+/* Tangent (forward sensitivity) solve (dR/dQ) dq = b with the exact Jacobian,
+ * the dual of st_adjoint_solve_device; used to cross-check adjoint gradients. */
+int st_tangent_solve_device(st_ctx* ctx, const double* b_dev, double* dq_dev, double cfl_prec, int krylov_m,
+                            int maxit, double rtol, st_solve_stats* stats);
+
 /* Kernel launches one st_residual_device / st_vjp_device call makes. */
 int st_launch_counts(st_ctx* ctx, int lhs, int* residual, int* vjp);
 

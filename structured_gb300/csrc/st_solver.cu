@@ -870,4 +870,21 @@ int st_adjoint_solve_device(st_ctx* x, const double* b_dev, double* psi_dev, dou
     return gmres(x, op, b_dev, psi_dev, krylov_m, maxit, rtol, stats);
 }
 
+int st_tangent_solve_device(st_ctx* x, const double* b_dev, double* dq_dev, double cfl_prec, int krylov_m, int maxit,
+                            double rtol, st_solve_stats* stats) {
+    if (!x || !b_dev || !dq_dev) return fail(ST_ERR_ARG, "st_tangent_solve_device: null argument");
+    if (krylov_m < 1 || krylov_m > 500 || maxit < 1) return fail(ST_ERR_ARG, "st_tangent_solve_device: krylov sizes");
+    for (const auto& b : x->bcs)
+        if (b.type == ST_BC_PERIODIC || b.type == ST_BC_WAKE)
+            return fail(ST_ERR_UNSUPPORTED, "st_tangent_solve_device: periodic/wake boundaries couple distant cells");
+    int rc = assemble_pair(x, x->c.order);
+    if (rc) return rc;
+    rc = stx::run_dt(x, cfl_prec);
+    if (rc) return rc;
+    LinOp op{false, 0.0, 1.0, nullptr, -1.0, x->dt};
+    rc = factor_M(x, op);
+    if (rc) return rc;
+    return gmres(x, op, b_dev, dq_dev, krylov_m, maxit, rtol, stats);
+}
+
 }  // extern "C"

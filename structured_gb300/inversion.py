@@ -1,0 +1,164 @@
+"""Adjoint-driven field inversion of the SA production multiplier beta.
+
+Objective (per case):  f(beta) = sum_i (Cf_i - Cf*_i)^2 + lam * sum_c (beta_c - 1)^2,
+Cf over the no-slip plate's wall faces.  Gradient by the discrete adjoint:
+    (dR/dQ)^T psi = (df/dQ)^T,      df/dbeta = 2 lam (beta - 1) - (dR/dbeta)^T psi,
+every piece on the GPU through the C ABI (flow solve: st_solve; df/dQ:
+st_cf_gradient_device; adjoint: st_adjoint_solve_device; (dR/dbeta)^T psi:
+st_vjp_device).  The optimiser is L-BFGS (two-loop recursion, Armijo
+backtracking) on the host over the beta field.  The reference has no
+adjoint, objective or inversion; this module is new.
+"""
+from __future__ import annotations
+
+import dataclasses
+import time
+
+import numpy as np
+
+from .solver import EulerEquation, Solver
+
+
+def plate_weights(case, xv) -> np.ndarray:
+    """dx of each bottom face on the plate (zero elsewhere): drag J = sum w Cf."""
+    w = np.zeros(case.nic)
+    lo = max(case.i_le, 0)
+    for i in range(lo, case.nic):
+        xm = 0.5 * (xv[i, 0] + xv[i + 1, 0])
+        if xm <= case.plate_x_end:
+            w[i] = xv[i + 1, 0] - xv[i, 0]
+    return w
+
+
+def plate_mask(case, xv) -> np.ndarray:
+    return plate_weights(case, xv) > 0
+
+
+SOLVE_COLD = dict(max_steps=400, cfl=5.0, cfl_ramp=1, cfl_ramp_iteration=3, cfl_ramp_exponent=1.2,
+                  rel_tolerance=1e-12, krylov_rtol=1e-4, krylov_m=60, krylov_maxit=300)
+SOLVE_WARM = dict(max_steps=60, cfl=1e3, cfl_ramp=1, cfl_ramp_iteration=0, cfl_ramp_exponent=1.5, min_steps=1,
+                  krylov_rtol=1e-6, krylov_m=60, krylov_maxit=300)
+
+
+def converge(eq: EulerEquation, q0=None, warm=False, tol_abs=None, **over):
+    """Pseudo-time Newton to steady state; returns (ok, history)."""
+    if q0 is not None:
+        eq.set_state(q0)
+    params = dict(SOLVE_WARM if warm else SOLVE_COLD)
+    if tol_abs is not None:
+        params.update(tolerance=tol_abs, rel_tolerance=0.0)
+    params.update(over)
+    return Solver(eq, **params).solve(raise_on_noconv=False)
+
+
+def cf_adjoint_gradient(eq: EulerEquation, w: np.ndarray, rtol: float = 1e-10):
+    """d(sum_i w_i Cf_i)/dbeta at the converged state of eq (beta as set).
+    Returns (grad [nic][njc], adjoint stats)."""
+    import torch
+    shape = eq.shape
+    g = torch.zeros(shape, dtype=torch.float64, device="cuda")
+    eq.cf_gradient_device(w, g.data_ptr())
+    psi = torch.zeros_like(g)
+    st = eq.adjoint_solve_device(g.data_ptr(), psi.data_ptr(), rtol=rtol)
+    oq = torch.empty_like(g)
+    ob = torch.empty((eq.nic, eq.njc), dtype=torch.float64, device="cuda")
+    eq.vjp_device(psi.data_ptr(), oq.data_ptr(), ob.data_ptr())
+    torch.cuda.synchronize()
+    return -ob.cpu().numpy(), st
+
+
+@dataclasses.dataclass
+class InversionResult:
+    beta: np.ndarray
+    q: np.ndarray
+    cf: np.ndarray
+    f_history: list
+    misfit_history: list
+    iterations: int
+    wall_s: float
+    flow_solves: int
+
+
+def invert(eq: EulerEquation, xv: np.ndarray, cf_target: np.ndarray, q_start: np.ndarray, lam: float = 1e-4,
+           max_iter: int = 40, m: int = 10, gtol: float = 1e-10, log=print) -> InversionResult:
+    """L-BFGS over beta for f = |Cf - Cf*|^2 + lam |beta - 1|^2 on the plate faces."""
+    case = eq.case
+    mask = plate_mask(case, xv)
+    t0 = time.time()
+    solves = [0]
+    state = {"q": q_start.copy()}
+
+    def evaluate(beta):
+        eq.set_beta(beta)
+        ok, _ = converge(eq, state["q"], warm=True)
+        solves[0] += 1
+        if not ok:
+            ok, _ = converge(eq, state["q"], warm=False)
+            solves[0] += 1
+            if not ok:
+                return np.inf, None, None, None
+        q = eq.get_state()
+        cf, _ = eq.skin_friction()
+        r = np.where(mask, cf - cf_target, 0.0)
+        misfit = float((r * r).sum())
+        f = misfit + lam * float(((beta - 1.0) ** 2).sum())
+        g, _ = cf_adjoint_gradient(eq, 2.0 * r)
+        g = g + 2.0 * lam * (beta - 1.0)
+        return f, g, q, (misfit, cf)
+
+    beta = np.ones((case.nic, case.njc))
+    f, g, q, extra = evaluate(beta)
+    if g is None:
+        raise RuntimeError("flow solve failed at beta = 1")
+    state["q"] = q
+    fh, mh = [f], [extra[0]]
+    S, Y = [], []
+    it = 0
+    for it in range(1, max_iter + 1):
+        # two-loop recursion
+        d = -g.copy()
+        alphas = []
+        for s, y in reversed(list(zip(S, Y))):
+            a = (s * d).sum() / (y * s).sum()
+            alphas.append(a)
+            d -= a * y
+        if S:
+            s, y = S[-1], Y[-1]
+            d *= (s * y).sum() / (y * y).sum()
+        else:
+            d *= 1e-2 / max(np.abs(g).max(), 1e-300)
+        for (s, y), a in zip(zip(S, Y), reversed(alphas)):
+            b = (y * d).sum() / (y * s).sum()
+            d += (a - b) * s
+        gd = float((g * d).sum())
+        if gd >= 0:
+            d, gd = -g, -float((g * g).sum())
+            S, Y = [], []
+        step, accepted = 1.0, False
+        for _ls in range(8):
+            bn = beta + step * d
+            fn, gn, qn, extra_n = evaluate(bn)
+            if gn is not None and fn <= f + 1e-4 * step * gd:
+                accepted = True
+                break
+            step *= 0.3
+        if not accepted:
+            log("inversion: line search failed at iteration %d" % it)
+            break
+        S.append(bn - beta)
+        Y.append(gn - g)
+        if len(S) > m:
+            S.pop(0)
+            Y.pop(0)
+        beta, f, g, state["q"] = bn, fn, gn, qn
+        fh.append(f)
+        mh.append(extra_n[0])
+        log("inversion it %3d  f %.6e  misfit %.6e  |g| %.3e  step %.2e  solves %d" %
+            (it, f, extra_n[0], np.abs(g).max(), step, solves[0]))
+        if np.abs(g).max() < gtol:
+            break
+    eq.set_beta(beta)
+    eq.set_state(state["q"])
+    cf, _ = eq.skin_friction()
+    return InversionResult(beta=beta, q=state["q"], cf=cf, f_history=fh, misfit_history=mh, iterations=it,
+                           wall_s=time.time() - t0, flow_solves=solves[0])

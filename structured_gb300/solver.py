@@ -83,6 +83,7 @@ def load_library() -> ctypes.CDLL:
                          ctypes.POINTER(I)]),
         "st_cf_gradient_device": (I, [V, _P, V]),
         "st_adjoint_solve_device": (I, [V, V, V, D, I, I, D, ctypes.POINTER(abi.StSolveStats)]),
+        "st_tangent_solve_device": (I, [V, V, V, D, I, I, D, ctypes.POINTER(abi.StSolveStats)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -340,8 +341,14 @@ def _eq_extras():
                                                 float(rtol), ctypes.byref(st)), "st_adjoint_solve_device")
         return st
 
+    def tangent_solve_device(self, b_ptr, dq_ptr, cfl_prec=1e6, m=60, maxit=600, rtol=1e-10):
+        st = abi.StSolveStats()
+        _check(self.lib.st_tangent_solve_device(self.h, _vp(b_ptr), _vp(dq_ptr), float(cfl_prec), m, maxit,
+                                                float(rtol), ctypes.byref(st)), "st_tangent_solve_device")
+        return st
+
     for f in (jacobian_assemble, jacobian_blocks, jacobian_apply_device, linear_solve_device, cf_gradient_device,
-              adjoint_solve_device):
+              adjoint_solve_device, tangent_solve_device):
         setattr(EulerEquation, f.__name__, f)
 
 
