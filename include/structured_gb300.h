@@ -92,7 +92,12 @@ typedef struct st_solve_params {
     double rel_tolerance;                 /* ... or <= rel_tolerance * initial */
     double krylov_rtol;
     double ser_exponent;                  /* > 0: also CFL >= cfl (r0/r)^ser_exponent */
-    double divergence_factor;             /* residual growth over the best seen that counts as divergence */
+    double divergence_factor;             /* unused (kept for layout); see reject_factor */
+    double cfl_growth;                    /* > 0: CFL *= cfl_growth after each accepted full step */
+    double reject_factor;                 /* a step that raises max ||R|| by more than this is undone, CFL / 10 */
+    double max_rel_drho;                  /* > 0: damp the update so |d rho / rho| <= this in every cell */
+    double nut_floor;                     /* SA: rho nu_tilde keeps at least this fraction of its old value */
+    double cfl_min;                       /* lower bound for CFL cuts */
 } st_solve_params;
 
 const char* st_last_error(void);

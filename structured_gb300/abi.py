@@ -76,4 +76,6 @@ class StSolveParams(ctypes.Structure):
                 ("cfl", ctypes.c_double), ("cfl_max", ctypes.c_double), ("cfl_ramp_exponent", ctypes.c_double),
                 ("under_relaxation", ctypes.c_double), ("under_relaxation_ramp_exponent", ctypes.c_double),
                 ("tolerance", ctypes.c_double), ("rel_tolerance", ctypes.c_double), ("krylov_rtol", ctypes.c_double),
-                ("ser_exponent", ctypes.c_double), ("divergence_factor", ctypes.c_double)]
+                ("ser_exponent", ctypes.c_double), ("divergence_factor", ctypes.c_double),
+                ("cfl_growth", ctypes.c_double), ("reject_factor", ctypes.c_double),
+                ("max_rel_drho", ctypes.c_double), ("nut_floor", ctypes.c_double), ("cfl_min", ctypes.c_double)]

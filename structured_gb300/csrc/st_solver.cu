@@ -374,6 +374,7 @@ __global__ void __launch_bounds__(256) k_ilu_solve(int nic, int njc, const doubl
 // Krylov vector kernels: deterministic multi-dot (fixed grid, fixed tree)
 // ---------------------------------------------------------------------------
 constexpr int DOT_BLOCKS = 128;
+constexpr int NORM_PART_BLOCKS = 128;
 __global__ void __launch_bounds__(256) k_mdot_part(const double* __restrict__ V, size_t n, const double* __restrict__ w,
                                                    double* __restrict__ part) {
     const int vi = blockIdx.y;
@@ -451,6 +452,31 @@ __global__ void k_cf_adj(DevCase c, const double* __restrict__ w, double scale, 
     double* o = Pbar + pidx(c, ip, jp);
     o[P_U] += ub;
     o[P_V] += vb;
+}
+
+// per-block max of |dq_0 / q_0| (density change), deterministic
+__global__ void k_max_rel_drho(size_t ncell, int nq, const double* __restrict__ q, const double* __restrict__ dq,
+                               double* __restrict__ part) {
+    double m = 0.0;
+    for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncell; c += (size_t)gridDim.x * blockDim.x)
+        m = fmax(m, fabs(dq[c * nq] / q[c * nq]));
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_down_sync(0xffffffffu, m, o));
+    __shared__ double sm[8];
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double r = 0.0;
+        for (int k = 0; k < 8; k++) r = fmax(r, sm[k]);
+        part[blockIdx.x] = r;
+    }
+}
+// SA: rho nu_tilde keeps at least `frac` of its previous value
+__global__ void k_nut_floor(size_t ncell, double* __restrict__ q, const double* __restrict__ qold, double frac) {
+    for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncell; c += (size_t)gridDim.x * blockDim.x) {
+        const double o = qold[c * 5 + 4];
+        const double lo = o > 0.0 ? frac * o : o;
+        if (q[c * 5 + 4] < lo) q[c * 5 + 4] = lo;
+    }
 }
 
 template <class T>
@@ -763,37 +789,39 @@ int st_solve(st_ctx* x, const st_solve_params* p, st_solve_stats* stats, double*
     const unsigned g = grid_for(n);
     cudaStream_t s = x->stream;
     double cfl = p->cfl, omega = p->under_relaxation;
-    double r0 = -1.0, rbest = 1e300;
     std::vector<double> nrm(nq);
-    int step = 0, hist = 0, fails = 0;
+    auto residual_norm = [&](double* out) -> int {
+        int r = stx::run_residual(x, x->q, x->beta, x->rhs, x->c.order);
+        if (r) return r;
+        x->have_residual = true;
+        r = stx::run_norms(x, x->rhs, nrm.data());
+        if (r && r != ST_ERR_NONFINITE) return r;
+        double m = 0.0;
+        for (int k = 0; k < nq; k++) m = std::max(m, nrm[k]);
+        *out = (r == ST_ERR_NONFINITE) ? NAN : m;
+        return ST_OK;
+    };
+    double rn;
+    rc = residual_norm(&rn);
+    if (rc) return rc;
+    if (!std::isfinite(rn)) return fail(ST_ERR_NONFINITE, "st_solve: non-finite initial residual");
+    const double r0 = rn;
+    int hist = 0, fails = 0, step = 0, accepted = 0;
     bool converged = false;
     st_solve_stats ls{};
-    for (; step <= p->max_steps; step++) {
-        rc = stx::run_residual(x, x->q, x->beta, x->rhs, x->c.order);
-        if (rc) return rc;
-        x->have_residual = true;
-        rc = stx::run_norms(x, x->rhs, nrm.data());
-        double rn = 0.0;
-        for (int k = 0; k < nq; k++) rn = std::max(rn, nrm[k]);
-        const bool bad = (rc == ST_ERR_NONFINITE) || (r0 > 0 && rn > p->divergence_factor * rbest);
-        if (rc && rc != ST_ERR_NONFINITE) return rc;
-        if (bad) {
-            // divergence guard: back to the last accepted state, smaller CFL
-            if (step == 0 || ++fails > p->max_failures) return fail(ST_ERR_NONFINITE, "st_solve: diverged");
-            ST_CUDA(cudaMemcpyAsync(x->q, x->qsave, n * 8, cudaMemcpyDeviceToDevice, s));
-            cfl = std::max(p->cfl, cfl * 0.1);
-            continue;
-        }
-        if (r0 < 0) r0 = rn;
-        rbest = std::min(rbest, rn);
+    auto record = [&]() {
         if (history && hist + nq + 3 <= history_len) {
-            history[hist++] = step;
+            history[hist++] = accepted;
             history[hist++] = cfl;
             history[hist++] = ls.iterations;
             for (int k = 0; k < nq; k++) history[hist++] = nrm[k];
         }
-        if (step >= p->min_steps && (rn <= p->tolerance || rn <= p->rel_tolerance * r0)) { converged = true; break; }
-        if (step == p->max_steps) break;
+    };
+    record();
+    std::vector<double> part(NORM_PART_BLOCKS);
+    for (step = 0; step < p->max_steps + p->max_failures; step++) {
+        if (accepted >= p->min_steps && (rn <= p->tolerance || rn <= p->rel_tolerance * r0)) { converged = true; break; }
+        if (accepted >= p->max_steps) break;
         rc = stx::run_dt(x, cfl);
         if (rc) return rc;
         rc = assemble_pair(x, x->c.lhs_order);
@@ -804,18 +832,47 @@ int st_solve(st_ctx* x, const st_solve_params* p, st_solve_stats* stats, double*
         ST_CUDA(cudaMemsetAsync(x->dq, 0, n * 8, s));
         rc = gmres(x, op, x->rhs, x->dq, p->krylov_m, p->krylov_maxit, p->krylov_rtol, &ls);
         if (rc) return rc;
+        double om = omega;
+        if (p->max_rel_drho > 0.0) {
+            k_max_rel_drho<<<NORM_PART_BLOCKS, 256, 0, s>>>(x->ncell, nq, x->q, x->dq, x->kpart);
+            ST_CUDA(cudaMemcpyAsync(part.data(), x->kpart, NORM_PART_BLOCKS * 8, cudaMemcpyDeviceToHost, s));
+            ST_CUDA(cudaStreamSynchronize(s));
+            double mx = 0.0;
+            for (double v : part) mx = std::max(mx, v);
+            if (mx * om > p->max_rel_drho) om = p->max_rel_drho / mx;
+        }
         ST_CUDA(cudaMemcpyAsync(x->qsave, x->q, n * 8, cudaMemcpyDeviceToDevice, s));
-        k_axpby<<<g, 256, 0, s>>>(n, omega, x->dq, 1.0, x->q);
+        k_axpby<<<g, 256, 0, s>>>(n, om, x->dq, 1.0, x->q);
+        if (nq == 5 && p->nut_floor > 0.0) k_nut_floor<<<grid_for(x->ncell), 256, 0, s>>>(x->ncell, x->q, x->qsave, p->nut_floor);
         ST_LAUNCH_CHECK("update");
-        // ramps of Solver::solve (src/solver/solver.cpp:212-230)
-        if (p->cfl_ramp && step + 1 > p->cfl_ramp_iteration) cfl = std::min(std::pow(cfl, p->cfl_ramp_exponent), p->cfl_max);
+        double rt;
+        rc = residual_norm(&rt);
+        if (rc) return rc;
+        if (!std::isfinite(rt) || rt > p->reject_factor * rn) {
+            // undo the step, smaller CFL
+            if (++fails > p->max_failures) return fail(ST_ERR_NONFINITE, "st_solve: diverged");
+            ST_CUDA(cudaMemcpyAsync(x->q, x->qsave, n * 8, cudaMemcpyDeviceToDevice, s));
+            cfl = std::max(p->cfl_min, cfl * 0.1);
+            rc = residual_norm(&rn);
+            if (rc) return rc;
+            continue;
+        }
+        rn = rt;
+        accepted++;
+        record();
+        if (p->cfl_growth > 0.0) {
+            if (om >= omega) cfl = std::min(p->cfl_max, cfl * p->cfl_growth);
+        } else if (p->cfl_ramp && accepted > p->cfl_ramp_iteration) {
+            // ramp of Solver::solve (src/solver/solver.cpp:212-220)
+            cfl = std::min(std::pow(cfl, p->cfl_ramp_exponent), p->cfl_max);
+        }
         if (p->ser_exponent > 0.0) cfl = std::min(p->cfl_max, std::max(cfl, p->cfl * std::pow(r0 / std::max(rn, 1e-300), p->ser_exponent)));
-        if (p->under_relaxation_ramp && step + 1 > p->under_relaxation_ramp_iteration)
-            omega = std::min(std::pow(omega, p->under_relaxation_ramp_exponent), 10.0);
+        if (p->under_relaxation_ramp && accepted > p->under_relaxation_ramp_iteration)
+            omega = std::min(std::pow(omega, p->under_relaxation_ramp_exponent), 10.0);  // solver.cpp:222-230
     }
     ST_CUDA(cudaStreamSynchronize(s));
     if (stats) *stats = ls;
-    if (steps_done) *steps_done = step;
+    if (steps_done) *steps_done = accepted;
     if (!converged) return fail(ST_ERR_NOCONV, "st_solve: tolerance not reached");
     return ST_OK;
 }

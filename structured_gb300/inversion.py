@@ -34,10 +34,10 @@ def plate_mask(case, xv) -> np.ndarray:
     return plate_weights(case, xv) > 0
 
 
-SOLVE_COLD = dict(max_steps=400, cfl=5.0, cfl_ramp=1, cfl_ramp_iteration=3, cfl_ramp_exponent=1.2,
-                  rel_tolerance=1e-12, krylov_rtol=1e-4, krylov_m=60, krylov_maxit=300)
-SOLVE_WARM = dict(max_steps=60, cfl=1e3, cfl_ramp=1, cfl_ramp_iteration=0, cfl_ramp_exponent=1.5, min_steps=1,
-                  krylov_rtol=1e-6, krylov_m=60, krylov_maxit=300)
+SOLVE_COLD = dict(max_steps=300, cfl=5.0, cfl_growth=2.0, rel_tolerance=1e-12, krylov_rtol=1e-4, krylov_m=60,
+                  krylov_maxit=300)
+SOLVE_WARM = dict(max_steps=60, cfl=1e4, cfl_growth=10.0, min_steps=1, rel_tolerance=1e-12, krylov_rtol=1e-6,
+                  krylov_m=60, krylov_maxit=300)
 
 
 def converge(eq: EulerEquation, q0=None, warm=False, tol_abs=None, **over):
@@ -80,8 +80,11 @@ class InversionResult:
 
 
 def invert(eq: EulerEquation, xv: np.ndarray, cf_target: np.ndarray, q_start: np.ndarray, lam: float = 1e-4,
-           max_iter: int = 40, m: int = 10, gtol: float = 1e-10, log=print) -> InversionResult:
-    """L-BFGS over beta for f = |Cf - Cf*|^2 + lam |beta - 1|^2 on the plate faces."""
+           max_iter: int = 40, m: int = 10, gtol: float = 1e-10, log=print, tol_abs: float | None = None
+           ) -> InversionResult:
+    """L-BFGS over beta for f = |Cf - Cf*|^2 + lam |beta - 1|^2 on the plate faces.
+    tol_abs: absolute residual tolerance of the warm-started flow solves
+    (default: 1e-11 of the residual of q_start's freestream start)."""
     case = eq.case
     mask = plate_mask(case, xv)
     t0 = time.time()
@@ -90,10 +93,10 @@ def invert(eq: EulerEquation, xv: np.ndarray, cf_target: np.ndarray, q_start: np
 
     def evaluate(beta):
         eq.set_beta(beta)
-        ok, _ = converge(eq, state["q"], warm=True)
+        ok, _ = converge(eq, state["q"], warm=True, tol_abs=tol_abs)
         solves[0] += 1
         if not ok:
-            ok, _ = converge(eq, state["q"], warm=False)
+            ok, _ = converge(eq, state["q"], warm=False, tol_abs=tol_abs)
             solves[0] += 1
             if not ok:
                 return np.inf, None, None, None

@@ -277,8 +277,13 @@ def solve_params(case: C.Case | None = None, **over) -> abi.StSolveParams:
     p.rel_tolerance = 0.0
     p.ser_exponent = 0.0
     p.divergence_factor = 1e4
-    p.max_failures = 5
+    p.max_failures = 20
     p.min_steps = 0
+    p.cfl_growth = 0.0
+    p.reject_factor = 3.0
+    p.max_rel_drho = 0.3
+    p.nut_floor = 1e-3
+    p.cfl_min = 0.1
     for k, v in over.items():
         setattr(p, k, v)
     return p
