@@ -96,7 +96,8 @@ typedef struct st_solve_params {
     double cfl_growth;                    /* > 0: CFL *= cfl_growth after each accepted full step */
     double reject_factor;                 /* a step that raises max ||R|| by more than this is undone, CFL / 10 */
     double max_rel_drho;                  /* > 0: damp the update so |d rho / rho| <= this in every cell */
-    double nut_floor;                     /* SA: rho nu_tilde keeps at least this fraction of its old value */
+    double nut_floor;                     /* > 0, SA: rho nu_tilde keeps at least this fraction of its old
+                                             value (0 = off: converged SA-neg states may hold nu_tilde < 0) */
     double cfl_min;                       /* lower bound for CFL cuts */
 } st_solve_params;
 

@@ -40,6 +40,8 @@ constexpr double GAMMA = 1.4;
 constexpr double SA_CB1 = 0.1355, SA_CB2 = 0.622, SA_SIGMA = 2.0 / 3.0, SA_KAPPA = 0.41;
 constexpr double SA_CW2 = 0.3, SA_CW3 = 2.0, SA_CV1 = 7.1, SA_CV2 = 0.7, SA_CV3 = 0.9;
 constexpr double SA_CW1 = SA_CB1 / (SA_KAPPA * SA_KAPPA) + (1.0 + SA_CB2) / SA_SIGMA;
+// negative-nu_tilde branch (SA-neg: Allmaras, Johnson & Spalart, ICCFD7-1902, 2012)
+constexpr double SA_CT3 = 1.2, SA_CN1 = 16.0;
 constexpr double PR_TURB = 0.9;
 
 struct PCase {
@@ -563,6 +565,9 @@ void viscous_flux(const PCase& pc, const double* normal, int nfaces, const std::
 // SA source for one cell (per unit volume): rho*(beta*P - D) + cb2/sigma*rho*|grad nut|^2.
 template <class T>
 T sa_source(const T& rho, const T& nut, const T& mu, double d, const T& omega, const T& gnut2, const T& beta) {
+    if (nut < 0.0)  // SA-neg: P = cb1 (1 - ct3) Omega nut, D = -cw1 (nut / d)^2
+        return rho * (beta * SA_CB1 * (1.0 - SA_CT3) * omega * nut + SA_CW1 * (nut * nut) / (d * d))
+             + (SA_CB2 / SA_SIGMA) * rho * gnut2;
     const double k2d2 = SA_KAPPA * SA_KAPPA * d * d;
     const T nu = mu / rho;
     const T chi = nut / nu;
@@ -658,10 +663,13 @@ void residual(const PCase& pc, const T* q, const T* beta, T* rhs, int order, Wor
                 T chi = w.nut[g] / nu;
                 T chi3 = chi * chi * chi;
                 T fv1 = chi3 / (chi3 + SA_CV1 * SA_CV1 * SA_CV1);
-                T mut = w.rho[g] * w.nut[g] * fv1;
+                // SA-neg below nu_tilde = 0: mu_t = 0, diffusion rho nu_tilde f_n(chi)
+                const bool neg = w.nut[g] < 0.0;
+                T mut = neg ? T(0.0) : w.rho[g] * w.nut[g] * fv1;
+                T fn = neg ? (SA_CN1 + chi3) / (SA_CN1 - chi3) : T(1.0);
                 w.mu[g] = mu + mut;
                 w.k[g] = pc.cp * (mu / pc.c.pr_inf + mut / PR_TURB);
-                w.mud[g] = mu + w.rho[g] * w.nut[g];
+                w.mud[g] = mu + w.rho[g] * w.nut[g] * fn;
             } else {
                 w.mu[g] = mu;
                 w.k[g] = mu * pc.cp / pc.c.pr_inf;  // get_thermal_conductivity, fluid.cpp:44-46

@@ -188,6 +188,17 @@ __device__ inline void roe_rev(const RoeTape& t, const double* fb, double* bl, d
 __device__ inline double sa_source_adj(double rho, double nut, double mu, double d, double omega, double gnut2,
                                        double beta, double sb, double* rho_, double* nut_, double* mu_,
                                        double* omega_, double* gnut2_, double* beta_) {
+    if (nut < 0.0) {  // SA-neg branch of sa_source
+        const double cp = SA_CB1 * (1.0 - SA_CT3), id2 = 1.0 / (d * d);
+        const double src = beta * cp * omega * nut + SA_CW1 * nut * nut * id2;
+        *rho_ = sb * (src + (SA_CB2 / SA_SIGMA) * gnut2);
+        *nut_ = sb * rho * (beta * cp * omega + 2.0 * SA_CW1 * nut * id2);
+        *mu_ = 0.0;
+        *omega_ = sb * rho * beta * cp * nut;
+        *gnut2_ = sb * rho * (SA_CB2 / SA_SIGMA);
+        *beta_ = sb * rho * cp * omega * nut;
+        return rho * src + (SA_CB2 / SA_SIGMA) * rho * gnut2;
+    }
     const double k2d2 = SA_KAPPA * SA_KAPPA * d * d;
     const double chi = rho * nut / mu;
     const double chi3 = chi * chi * chi;
@@ -443,9 +454,9 @@ __global__ void __launch_bounds__(256) k_face_fused(DevCase c, const double* __r
                 double dndx, dndy, nb_;
                 ST_GRAD_D(P_NUT, dndx, dndy, nb_)
                 (void)nb_;
-                const double rnb = 0.375 * (pL[P_RHO] * pL[P_NUT] + pR[P_RHO] * pR[P_NUT])
-                                 + 0.0625 * (pPa[P_RHO] * pPa[P_NUT] + pPb[P_RHO] * pPb[P_NUT]
-                                             + pMa[P_RHO] * pMa[P_NUT] + pMb[P_RHO] * pMb[P_NUT]);
+#define ST_SD(p) sa_diff(p[P_RHO], p[P_NUT], p[P_MU])
+                const double rnb = 0.375 * (ST_SD(pL) + ST_SD(pR)) + 0.0625 * (ST_SD(pPa) + ST_SD(pPb) + ST_SD(pMa) + ST_SD(pMb));
+#undef ST_SD
                 const double cs = 1.0 / SA_SIGMA;
                 const double gdn = dndx * nx + dndy * ny;
                 f[4] -= cs * (mub + rnb) * gdn;
@@ -535,6 +546,8 @@ __global__ void __launch_bounds__(256) k_gather(DevCase c, const double* __restr
 #pragma unroll
         for (int s = 0; s < NP; s++) acc[s] = 0.0;
         const double* self = P + idx * NP;
+        double sd_r = 0.0, sd_n = 0.0, sd_m = 0.0;  // d (rho nut f_n) / d (rho, nut, mu) of this record
+        if (NQ == 5 && c.viscous) sa_diff_d(self[P_RHO], self[P_NUT], self[P_MU], &sd_r, &sd_n, &sd_m);
         auto visc = [&](const double* r, const double* gm, int role) {
             double wx, wy, co;
             if (role == 0) { wx = gm[G_WLX]; wy = gm[G_WLY]; co = 0.375; }
@@ -547,8 +560,9 @@ __global__ void __launch_bounds__(256) k_gather(DevCase c, const double* __restr
             acc[P_MU] += r[A_MUB] * co;
             if (NQ == 5) {
                 acc[P_MUT] += r[A_MUTB] * co;
-                acc[P_NUT] += r[A_DNDX] * wx + r[A_DNDY] * wy + r[A_RNB] * co * self[P_RHO];
-                acc[P_RHO] += r[A_RNB] * co * self[P_NUT];
+                acc[P_NUT] += r[A_DNDX] * wx + r[A_DNDY] * wy + r[A_RNB] * co * sd_n;
+                acc[P_RHO] += r[A_RNB] * co * sd_r;
+                acc[P_MU] += r[A_RNB] * co * sd_m;
             }
         };
         // ---- i-faces (f, j): L=(f, j+1) R=(f+1, j+1) P=(f|f+1, j+2) M=(f|f+1, j)
@@ -692,7 +706,7 @@ __global__ void __launch_bounds__(1024) k_bc_adj(DevCase c, const double* __rest
             double* gb = Pbar + pidx(c, ip, jp);
             double mub = gb[P_MU];
             const double T = g[P_T], mu = g[P_MU];
-            if (NQ == 5 && mu != 0.0) {
+            if (NQ == 5 && mu != 0.0 && g[P_NUT] >= 0.0) {  // mu_t = 0 for nut < 0
                 const double s = g[P_RHO] * g[P_NUT];
                 const double chi = s / mu, chi3 = chi * chi * chi, den = chi3 + SA_CV1_3;
                 const double f = chi3 / den, fp = 3.0 * chi * chi * SA_CV1_3 / (den * den);
@@ -835,7 +849,7 @@ __global__ void __launch_bounds__(256) k_prim_adj(DevCase c, const double* __res
         double rhob = b[P_RHO], ub = b[P_U], vb = b[P_V], pb = b[P_P], Tb = b[P_T], nutb = b[P_NUT], mub = b[P_MU];
         if (c.viscous) {
             const double mu = p[P_MU];
-            if (NQ == 5) {
+            if (NQ == 5 && p[P_NUT] >= 0.0) {  // mu_t = 0 for nut < 0
                 const double s = rho * p[P_NUT];
                 const double chi = s / mu, chi3 = chi * chi * chi, den = chi3 + SA_CV1_3;
                 const double f = chi3 / den, fp = 3.0 * chi * chi * SA_CV1_3 / (den * den);

@@ -32,6 +32,8 @@ constexpr double SA_CW2 = 0.3, SA_CW3 = 2.0, SA_CV1 = 7.1, SA_CV2 = 0.7, SA_CV3 
 constexpr double SA_CW1 = SA_CB1 / (SA_KAPPA * SA_KAPPA) + (1.0 + SA_CB2) / SA_SIGMA;
 constexpr double SA_CV1_3 = SA_CV1 * SA_CV1 * SA_CV1;
 constexpr double SA_CW3_6 = SA_CW3 * SA_CW3 * SA_CW3 * SA_CW3 * SA_CW3 * SA_CW3;
+// negative-nu_tilde branch (SA-neg: Allmaras, Johnson & Spalart, ICCFD7-1902, 2012)
+constexpr double SA_CT3 = 1.2, SA_CN1 = 16.0;
 constexpr double PR_TURB = 0.9;
 
 // primitive record slots
@@ -122,12 +124,37 @@ __device__ inline T laminar_mu(const DevCase& c, T temp) {
     return c.mu_inf * (cb * cb);
 }
 
-// SA eddy viscosity mu_t = rho nu_tilde f_v1(chi), chi = rho nu_tilde / mu
+// SA eddy viscosity mu_t = rho nu_tilde f_v1(chi), chi = rho nu_tilde / mu;
+// zero for nu_tilde < 0 (SA-neg)
 template <class T>
 __device__ inline T sa_mut(T rho, T nut, T mu) {
+    if (val(nut) < 0.0) return T(0.0);
     T chi = rho * nut * rcp(mu);
     T chi3 = chi * chi * chi;
     return rho * nut * (chi3 * rcp(chi3 + SA_CV1_3));
+}
+
+// The nu_tilde part of the SA diffusion coefficient, rho nu_tilde f_n(chi):
+// f_n = 1 for nu_tilde >= 0, (c_n1 + chi^3) / (c_n1 - chi^3) below (SA-neg),
+// which keeps mu + rho nu_tilde f_n > 0.
+template <class T>
+__device__ inline T sa_diff(T rho, T nut, T mu) {
+    const T m = rho * nut;
+    if (val(nut) >= 0.0) return m;
+    const T chi = m * rcp(mu);
+    const T chi3 = chi * chi * chi;
+    return m * ((SA_CN1 + chi3) * rcp(SA_CN1 - chi3));
+}
+// its partial derivatives with respect to rho, nu_tilde and mu
+__device__ inline void sa_diff_d(double rho, double nut, double mu, double* d_rho, double* d_nut, double* d_mu) {
+    if (nut >= 0.0) { *d_rho = nut; *d_nut = rho; *d_mu = 0.0; return; }
+    const double m = rho * nut, chi = m / mu, chi3 = chi * chi * chi, den = SA_CN1 - chi3;
+    const double fn = (SA_CN1 + chi3) / den;
+    const double fnp = 6.0 * SA_CN1 * chi * chi / (den * den);  // d f_n / d chi
+    const double dm = fn + chi * fnp;
+    *d_rho = dm * nut;
+    *d_nut = dm * rho;
+    *d_mu = -chi * chi * fnp;
 }
 
 // bounded mbarrier / flag spin helper limit

@@ -398,9 +398,9 @@ __global__ void __launch_bounds__(256) k_face(DevCase c, const T* __restrict__ P
                 T dndx, dndy, nbar;
                 ST_GRAD(P_NUT, dndx, dndy, nbar)
                 (void)nbar;
-                const T rnb = 0.375 * (pL[P_RHO] * pL[P_NUT] + pR[P_RHO] * pR[P_NUT])
-                            + 0.0625 * (pPa[P_RHO] * pPa[P_NUT] + pPb[P_RHO] * pPb[P_NUT]
-                                        + pMa[P_RHO] * pMa[P_NUT] + pMb[P_RHO] * pMb[P_NUT]);
+#define ST_SD(p) sa_diff(p[P_RHO], p[P_NUT], p[P_MU])
+                const T rnb = 0.375 * (ST_SD(pL) + ST_SD(pR)) + 0.0625 * (ST_SD(pPa) + ST_SD(pPb) + ST_SD(pMa) + ST_SD(pMb));
+#undef ST_SD
                 f[4] = f[4] - (1.0 / SA_SIGMA) * (mub + rnb) * (dndx * nx + dndy * ny);
                 T* g = G + fi.face * 4;
                 g[0] = dudy; g[1] = dvdx; g[2] = dndx; g[3] = dndy;
@@ -414,9 +414,13 @@ __global__ void __launch_bounds__(256) k_face(DevCase c, const T* __restrict__ P
 }
 
 // SA source per unit volume: rho (beta P - D) + (cb2/sigma) rho |grad nut|^2,
-// P = cb1 S~ nut, D = cw1 fw (nut/d)^2 (Spalart & Allmaras 1992, SA-noft2).
+// P = cb1 S~ nut, D = cw1 fw (nut/d)^2 (Spalart & Allmaras 1992, SA-noft2);
+// for nut < 0 (SA-neg) P = cb1 (1 - ct3) Omega nut, D = -cw1 (nut/d)^2.
 template <class T>
 __device__ inline T sa_source(T rho, T nut, T mu, double d, T omega, T gnut2, T beta) {
+    if (val(nut) < 0.0)
+        return rho * (beta * (SA_CB1 * (1.0 - SA_CT3)) * omega * nut + SA_CW1 * (nut * nut) * (1.0 / (d * d)))
+             + (SA_CB2 / SA_SIGMA) * rho * gnut2;
     const double k2d2 = SA_KAPPA * SA_KAPPA * d * d;
     const T chi = rho * nut * rcp(mu);
     const T chi3 = chi * chi * chi;

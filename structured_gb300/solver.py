@@ -282,7 +282,7 @@ def solve_params(case: C.Case | None = None, **over) -> abi.StSolveParams:
     p.cfl_growth = 0.0
     p.reject_factor = 3.0
     p.max_rel_drho = 0.3
-    p.nut_floor = 1e-3
+    p.nut_floor = 0.0
     p.cfl_min = 0.1
     for k, v in over.items():
         setattr(p, k, v)

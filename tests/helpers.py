@@ -33,3 +33,16 @@ def flat_plate(tmp, name, ni, nj, **kw):
     args = dict(mach=0.3, reynolds=1e6, h1=1e-4, ratio=1.08)
     args.update(kw)
     return C.flat_plate_case(str(tmp), name, ni, nj, **args)
+
+
+def negative_nut_state(c, seed):
+    """perturbed_state with rho nu_tilde negative (-0.5..-12 x freestream, chi
+    down to about -36, across fv1's pole at chi = -c_v1) in a patch touching
+    the wall: exercises the SA-neg branches of mu_t, the diffusion coefficient
+    and the source."""
+    q = C.perturbed_state(c, seed)
+    rng = np.random.default_rng(seed + 1)
+    i0, i1, j1 = c.nic // 3, c.nic // 2 + 2, max(3, c.njc // 3)
+    patch = q[i0:i1, :j1, 4]
+    q[i0:i1, :j1, 4] = -np.abs(patch) * rng.uniform(0.5, 12.0, patch.shape)
+    return q

@@ -7,7 +7,7 @@ forward-mode JVP at full size."""
 import numpy as np
 import pytest
 
-from helpers import flat_plate, golden_names, load_golden
+from helpers import flat_plate, golden_names, load_golden, negative_nut_state
 from structured_gb300 import case as C
 
 pytestmark = pytest.mark.gpu
@@ -118,3 +118,24 @@ def test_fused_residual_adjoint_matches_separate_calls(gpu_lib, port_built, tmp_
     assert rel_err(rhs_b, rhs_a, port.flux_scale(q)) < 1e-13
     assert rel_err(rhs_b, port.residual(q), port.flux_scale(q)) < 1e-12
     assert np.array_equal(oq_a, oq_b) and np.array_equal(ob_a, ob_b)
+
+
+def test_sa_neg_vjp_matches_oracle(gpu_lib, port_built, tmp_path):
+    """The hand-written reverse of the SA-neg branches (mu_t = 0, rho nu_tilde
+    f_n in the diffusion coefficient, the negative source) against the
+    oracle's exact transposed products."""
+    from oracle.port import PortCase
+    c = flat_plate(tmp_path, "negv", 45, 29, turbulence="sa", viscosity_law="sutherland", reynolds=5e6, h1=1e-6,
+                   ratio=1.15, mach=0.2)
+    xv, yv = C.load_grid(c)
+    q = negative_nut_state(c, 47)
+    rng = np.random.default_rng(48)
+    beta = 1.0 + 0.2 * rng.standard_normal((c.nic, c.njc))
+    psi = rng.standard_normal(q.shape)
+    eq = eq_for(c, xv, yv)
+    eq.set_state(q)
+    eq.set_beta(beta)
+    oq, ob = eq.vjp(psi)
+    rq, rb = PortCase(c, xv, yv).vjp(q, psi, beta)
+    assert close(oq, rq) < TOL
+    assert close(ob, rb) < TOL

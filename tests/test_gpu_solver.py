@@ -89,7 +89,8 @@ def test_laminar_plate_converges_to_blasius(gpu_lib, tmp_path):
 
 def test_adjoint_gradient_matches_finite_differences(gpu_lib, tmp_path):
     """SA plate: dJ/dbeta from the adjoint solve vs central differences of
-    converged solves (step 1e-6) on seeded cells."""
+    converged solves (step 1e-6) on seeded cells, to 1e-5 relative above the
+    difference quotient's round-off floor."""
     import torch
     from structured_gb300.solver import Solver
     c = flat_plate(tmp_path, "fd", 49, 41, turbulence="sa", mach=0.2, reynolds=1e6, h1=1e-5, ratio=1.12,
@@ -118,8 +119,10 @@ def test_adjoint_gradient_matches_finite_differences(gpu_lib, tmp_path):
     eq.vjp_device(psi.data_ptr(), oq.data_ptr(), ob.data_ptr())
     torch.cuda.synchronize()
     grad = -ob.cpu().numpy()
+    # seeded cells among those whose gradient carries signal (>= 1 % of the largest)
     rng = np.random.default_rng(74)
-    cells = [(int(rng.integers(c.i_le + 2, c.nic - 2)), int(rng.integers(0, 12))) for _ in range(4)]
+    cand = np.argwhere(np.abs(grad) >= 1e-2 * np.abs(grad).max())
+    cells = [tuple(int(t) for t in cand[k]) for k in rng.choice(len(cand), size=4, replace=False)]
     h = 1e-6
     for (i, j) in cells:
         Js = []
@@ -133,7 +136,9 @@ def test_adjoint_gradient_matches_finite_differences(gpu_lib, tmp_path):
             assert ok, hs
             Js.append(eq.skin_friction()[1])
         fd = (Js[0] - Js[1]) / (2 * h)
-        assert abs(fd - grad[i, j]) <= 1e-6 * abs(grad).max() + 1e-5 * abs(fd), (i, j, fd, grad[i, j])
+        # round-off floor of the difference quotient: J to ~200 ulp over 2h
+        floor = 200 * np.finfo(float).eps * abs(J0) / (2 * h)
+        assert abs(fd - grad[i, j]) <= 1e-5 * abs(grad[i, j]) + floor, (i, j, fd, grad[i, j], floor)
     eq.set_beta(beta0)
 
 

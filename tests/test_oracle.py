@@ -4,7 +4,7 @@ import os
 import numpy as np
 import pytest
 
-from helpers import flat_plate, golden_names, load_golden, rel_err
+from helpers import flat_plate, golden_names, load_golden, negative_nut_state, rel_err
 from structured_gb300 import case as C
 
 
@@ -36,12 +36,13 @@ def test_port_matches_reference_live(port_built, ref_available, tmp_path):
     assert rel_err(p.residual(q), ref.residual(q), p.flux_scale(q)) < 1e-13
 
 
-@pytest.mark.parametrize("turb", ["none", "sa"])
+@pytest.mark.parametrize("turb", ["none", "sa", "sa_neg"])
 def test_port_jvp_matches_central_fd(port_built, tmp_path, turb):
+    """sa_neg: a patch of negative nu_tilde (the SA-neg branches)."""
     from oracle.port import PortCase
-    c = flat_plate(tmp_path, "jvp_" + turb, 25, 17, turbulence=turb)
+    c = flat_plate(tmp_path, "jvp_" + turb, 25, 17, turbulence=turb[:2] if turb != "none" else turb)
     p = PortCase(c)
-    q = C.perturbed_state(c, 5)
+    q = negative_nut_state(c, 5) if turb == "sa_neg" else C.perturbed_state(c, 5)
     rng = np.random.default_rng(1)
     v = rng.standard_normal(q.shape) * np.abs(q).mean(axis=(0, 1))
     beta = 1.0 + 0.1 * rng.standard_normal(q.shape[:2])
