@@ -525,13 +525,13 @@ int st_destroy(st_ctx* x) {
     double* bufs[] = {x->q, x->rhs, x->beta, x->P, x->lim, x->Fi, x->Fj, x->Gi, x->Gj, x->vol_d, x->ivol_d,
                       x->geo_i, x->geo_j, x->wd, x->nchi_d, x->neta_d, x->dsmin_d, x->dt, x->norm_part, x->norm_out,
                       x->cf, x->wall_dx_d, x->Pbar, x->srec, x->arec_i, x->arec_j, x->psi_tmp,
-                      x->outq_tmp, x->outb_tmp, x->tape, x->jac, x->jac1, x->lfac, x->kv, x->kz, x->kw, x->kr, x->kh, x->kpart, x->dq, x->qsave};
+                      x->outq_tmp, x->outb_tmp, x->tape, x->jac, x->jac1, x->kv, x->kzb, x->kz, x->kw, x->kr, x->kh, x->kpart, x->dq, x->qsave};
     for (double* b : bufs) if (b) cudaFree(b);
     st::dual* dbufs[] = {x->qd, x->Pd, x->limd, x->Fdi, x->Fdj, x->Gdi, x->Gdj, x->rhsd, x->betad};
     for (st::dual* b : dbufs) if (b) cudaFree(b);
     if (x->bcs_d) cudaFree(x->bcs_d);
     if (x->err_d) cudaFree(x->err_d);
-    if (x->bar_d) cudaFree(x->bar_d);
+    if (x->lfac) cudaFree(x->lfac);
     for (auto& e : x->ev) if (e) cudaEventDestroy(e);
     if (x->stream) cudaStreamDestroy(x->stream);
     delete x;

@@ -36,11 +36,12 @@ struct st_ctx {
     // adjoint buffers, allocated on the first VJP call
     double *Pbar = nullptr, *srec = nullptr, *arec_i = nullptr, *arec_j = nullptr;
     // implicit solver (allocated on first use)
-    double *jac = nullptr, *jac1 = nullptr, *lfac = nullptr, *kv = nullptr, *kz = nullptr, *kw = nullptr, *kr = nullptr;
+    double *jac = nullptr, *jac1 = nullptr, *kv = nullptr, *kz = nullptr, *kw = nullptr, *kr = nullptr;
     double *kh = nullptr, *kpart = nullptr, *dq = nullptr, *qsave = nullptr;
+    double* kzb = nullptr;   // flexible GMRES: preconditioned basis Z = M^{-1} V
+    float* lfac = nullptr;   // block ILU(0) factors, FP32: [cell][9][nq][nq]
     int kv_m = 0;
     bool jac1_is_jac = false;
-    unsigned* bar_d = nullptr;
     double *psi_tmp = nullptr, *outq_tmp = nullptr, *outb_tmp = nullptr, *tape = nullptr;
 
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
