@@ -219,6 +219,29 @@ int st_launch_counts(st_ctx* ctx, int lhs, int* residual, int* vjp);
  * race. */
 int st_norms_noalloc(const double* rhs_dev, long long ncell, int nq, double* out_dev, void* stream);
 
+/* ---- learned SA correction (no counterpart in the reference) -------------
+ * A 4-64-64-1 MLP (tanh, tanh, softplus) maps four features of each cell to
+ * the SA production multiplier beta: P/(P+D) with beta = 1, chi, log10 y+
+ * (u_tau from the wall shear of the cell's column) and |S|/|Omega|.  Weights
+ * are BF16, products run on the tensor cores with FP32 accumulation; the
+ * FP32 master copy is trained by Adam.  Enabled, the residual kernels of
+ * st_residual*, st_jvp_device and st_solve evaluate beta in-kernel from the
+ * current state (Jacobian products hold it fixed); the fused
+ * residual+adjoint pipeline keeps using the beta array. */
+int st_mlp_param_count(void);                                /* FP32 master parameters */
+int st_mlp_init(st_ctx* ctx, unsigned long long seed);       /* Xavier-uniform weights, zero biases */
+int st_mlp_set_params(st_ctx* ctx, const float* params);    /* [st_mlp_param_count()] */
+int st_mlp_get_params(st_ctx* ctx, float* params);
+int st_mlp_set_normalization(st_ctx* ctx, const float mean[4], const float stdev[4]);
+int st_mlp_enable(st_ctx* ctx, int on);
+/* Adam (lr, beta1 0.9, beta2 0.999) on (1/batch) sum (beta - target)^2 over
+ * batches drawn with replacement from n device samples (features [n][4],
+ * raw; targets [n]); loss_host (optional) receives one loss per step. */
+int st_mlp_train(st_ctx* ctx, const float* feat_dev, const float* target_dev, long n, int steps, int batch, float lr,
+                 unsigned long long seed, float* loss_host);
+int st_sa_features(st_ctx* ctx, float* feat_dev);           /* raw features of the state, [ncell][4] */
+int st_mlp_beta(st_ctx* ctx, double* beta_dev);             /* network beta of the state, [ncell] */
+
 /* Diagnostics: dense FP64 FMA throughput of this device (TFLOP/s). */
 int st_probe_fp64(st_ctx* ctx, double* tflops);
 /* Runs one pipeline on the context state (which = 0: residual; 1: adjoint VJP

@@ -304,7 +304,12 @@ int launch_forward(st_ctx* x, const DevCase& dc, const T* q, const T* beta, T* P
         k_face<T, NQ, 1, 1><<<grid_for(x->nfj), 256, 0, s>>>(dc, P, lim, Fj, Gj);
         stx::mark(x, "k_face_j");
     }
-    k_cell<T, NQ><<<gc, 256, 0, s>>>(dc, P, Fi, Fj, Gi, Gj, beta, rhs);
+    if constexpr (NQ == 5) {
+        if (dc.mlp_wb) k_cell<T, NQ, true><<<gc, 256, 0, s>>>(dc, P, Fi, Fj, Gi, Gj, beta, rhs);
+        else k_cell<T, NQ><<<gc, 256, 0, s>>>(dc, P, Fi, Fj, Gi, Gj, beta, rhs);
+    } else {
+        k_cell<T, NQ><<<gc, 256, 0, s>>>(dc, P, Fi, Fj, Gi, Gj, beta, rhs);
+    }
     stx::mark(x, "k_cell");
     ST_LAUNCH_CHECK("residual launch");
     return ST_OK;
@@ -513,6 +518,7 @@ int st_create(const st_case* c, const double* xv, const double* yv, int device, 
     dc.dpdx = c->dpdx; dc.dpdy = c->dpdy;
     dc.vol = x->vol_d; dc.ivol = x->ivol_d; dc.geo_i = x->geo_i; dc.geo_j = x->geo_j; dc.wd = x->wd;
     dc.nchi = x->nchi_d; dc.neta = x->neta_d; dc.bcs = x->bcs_d; dc.err = x->err_d;
+    dc.mlp_wb = nullptr; dc.mlp_wf = nullptr;
     cudaError_t e = cudaStreamSynchronize(x->stream);
     if (e != cudaSuccess) { st_destroy(x); return stx::cuda_fail(e, "st_create"); }
     *out = x;
@@ -532,6 +538,9 @@ int st_destroy(st_ctx* x) {
     if (x->bcs_d) cudaFree(x->bcs_d);
     if (x->err_d) cudaFree(x->err_d);
     if (x->lfac) cudaFree(x->lfac);
+    if (x->mlp_wb) cudaFree(x->mlp_wb);
+    float* fbufs[] = {x->mlp_wf, x->mlp_master, x->mlp_loss, x->mlp_part};
+    for (float* b : fbufs) if (b) cudaFree(b);
     for (auto& e : x->ev) if (e) cudaEventDestroy(e);
     if (x->stream) cudaStreamDestroy(x->stream);
     delete x;

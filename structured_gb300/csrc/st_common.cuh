@@ -61,6 +61,8 @@ struct DevCase {
     const double* neta;    // [nic][nj][2]
     const DevBC* bcs;      // [nbc]
     int* err;              // device error flag
+    const void* mlp_wb;    // learned beta: BF16 weight block (null: beta from the beta array)
+    const float* mlp_wf;   // its FP32 biases and feature normalisation
 };
 
 __host__ __device__ inline size_t pidx(const DevCase& c, int ip, int jp) {

@@ -40,6 +40,12 @@ struct st_ctx {
     double *kh = nullptr, *kpart = nullptr, *dq = nullptr, *qsave = nullptr;
     double* kzb = nullptr;   // flexible GMRES: preconditioned basis Z = M^{-1} V
     float* lfac = nullptr;   // block ILU(0) factors, FP32: [cell][9][nq][nq]
+    // learned SA correction: BF16 weights, FP32 biases + normalisation, FP32
+    // master parameters with Adam moments, training partials
+    void* mlp_wb = nullptr;
+    float *mlp_wf = nullptr, *mlp_master = nullptr, *mlp_loss = nullptr, *mlp_part = nullptr;
+    size_t mlp_part_n = 0;
+    int mlp_t = 0;
     int kv_m = 0;
     bool jac1_is_jac = false;
     double *psi_tmp = nullptr, *outq_tmp = nullptr, *outb_tmp = nullptr, *tape = nullptr;

@@ -5,6 +5,7 @@
 // evaluates each face once, but through >40 full-grid temporaries).
 #pragma once
 #include "st_common.cuh"
+#include "st_mlp.cuh"
 
 namespace st {
 
@@ -446,13 +447,31 @@ __device__ inline T sa_source(T rho, T nut, T mu, double d, T omega, T gnut2, T 
 // K6  cell assembly: flux differences (eulerequation.cpp:136-154, :5-20),
 //     SA source, body force (:22-29), division by volume (:223-230).
 // ----------------------------------------------------------------------------
-template <class T, int NQ>
+// MLP: beta of each cell from the learned correction (st_mlp.cuh), evaluated
+// in-kernel 32 cells per warp; the loop then runs over whole-warp tiles so
+// that every lane reaches the warp-wide MMAs.
+template <class T, int NQ, bool MLP = false>
 __global__ void __launch_bounds__(256) k_cell(DevCase c, const T* __restrict__ P, const T* __restrict__ Fi,
                                               const T* __restrict__ Fj, const T* __restrict__ Gi,
                                               const T* __restrict__ Gj, const T* __restrict__ beta,
                                               T* __restrict__ rhs) {
     const size_t n = (size_t)c.nic * c.njc;
-    for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += (size_t)gridDim.x * blockDim.x) {
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t base = (size_t)blockIdx.x * blockDim.x + (MLP ? (threadIdx.x & ~31u) : threadIdx.x); base < n;
+         base += stride) {
+        const size_t idx = MLP ? base + (threadIdx.x & 31) : base;
+        float mlp_beta = 1.f;
+        if constexpr (MLP) {
+            __shared__ __nv_bfloat16 s_x[8 * MLP_SX], s_h[8 * MLP_SH];
+            const int w = threadIdx.x >> 5;
+            float f[MLP_IN] = {0.f, 0.f, 0.f, 0.f};
+            if (idx < n) {
+                sa_features(c, P, Gj, (int)(idx / c.njc), (int)(idx % c.njc), f);
+                mlp_normalise(c.mlp_wf, f);
+            }
+            mlp_beta = mlp_warp_beta((const __nv_bfloat16*)c.mlp_wb, c.mlp_wf, f, s_x + w * MLP_SX, s_h + w * MLP_SH);
+            if (idx >= n) continue;
+        }
         const int i = (int)(idx / c.njc), j = (int)(idx % c.njc);
         const T* fs = Fj + ((size_t)i * c.nj + j) * NQ;
         const T* fn = fs + NQ;
@@ -473,7 +492,7 @@ __global__ void __launch_bounds__(256) k_cell(DevCase c, const T* __restrict__ P
             const T ny = 0.25 * (gw[3] + ge[3] + gs[3] + gn[3]);
             const T omega = tfabs(vx - uy);
             const T* pc = P + pidx(c, i + 1, j + 1);
-            const T bta = beta ? beta[idx] : T(1.0);
+            const T bta = MLP ? T((double)mlp_beta) : (beta ? beta[idx] : T(1.0));
             const T s = sa_source(pc[P_RHO], pc[P_NUT], pc[P_MU], c.wd[idx], omega, nx * nx + ny * ny, bta);
             r[NQ - 1] = r[NQ - 1] + s * vol;
         }

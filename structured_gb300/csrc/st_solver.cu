@@ -990,8 +990,9 @@ int st_solve(st_ctx* x, const st_solve_params* p, st_solve_stats* stats, double*
         double rt;
         rc = residual_norm(&rt);
         if (rc) return rc;
-        // near round-off (below 1e-9 of the initial residual) growth is noise, not divergence
-        if (!std::isfinite(rt) || (rt > p->reject_factor * rn && rt > 1e-9 * r0)) {
+        // growth near round-off (below 1e-9 of the initial residual) or below
+        // the absolute tolerance is noise, not divergence
+        if (!std::isfinite(rt) || (rt > p->reject_factor * rn && rt > std::max(1e-9 * r0, p->tolerance))) {
             // undo the step, smaller CFL
             if (++fails > p->max_failures) return fail(ST_ERR_NONFINITE, "st_solve: diverged");
             ST_CUDA(cudaMemcpyAsync(x->q, x->qsave, n * 8, cudaMemcpyDeviceToDevice, s));

@@ -1,0 +1,120 @@
+"""Learned SA correction: training data from field inversions, training, and
+the held-out comparison of plain SA, the inverted-beta solve and the learned
+solve.  The reference has no turbulence model, adjoint or learning; this
+module is new.
+
+    python -m structured_gb300.validate mlp --data DIR [--out file.json]
+
+DIR holds the inversion_<tag>_<ni>x<nj>.npz files the inversion run writes.
+Training pairs are (features of the inverted state, inverted beta) over all
+cells of the eight cases other than Re_L = 3e6 at -2 degrees.
+"""
+from __future__ import annotations
+
+import glob
+import os
+import re
+import tempfile
+import time
+
+import numpy as np
+
+HELD_OUT = "Re3e+06_a-2"
+
+
+def _case_of(path: str):
+    from . import workloads
+    m = re.search(r"inversion_(Re([0-9.e+]+)_a([+-][0-9]+))_(\d+)x(\d+)\.npz$", os.path.basename(path))
+    if not m:
+        raise ValueError("not an inversion file: %s" % path)
+    tag, re_l, ang, ni, nj = m.group(1), float(m.group(2)), float(m.group(3)), int(m.group(4)), int(m.group(5))
+    return tag, workloads.turbulent_plate(tempfile.mkdtemp(), ni, nj, re_l, ang, write_files=False)
+
+
+def _eq_for(path: str):
+    from .solver import EulerEquation
+    tag, c = _case_of(path)
+    d = np.load(path)
+    return tag, c, d, EulerEquation(c, d["xv"], d["yv"])
+
+
+def training_set(paths):
+    """Device tensors (features [N][4] float32, targets [N] float32)."""
+    import torch
+    feats, targets = [], []
+    for path in paths:
+        tag, c, d, eq = _eq_for(path)
+        eq.set_state(d["q_inv"])
+        eq.set_beta(d["beta_inv"])
+        f = torch.empty((eq.nic * eq.njc, 4), dtype=torch.float32, device="cuda")
+        eq.sa_features_device(f.data_ptr())
+        feats.append(f)
+        targets.append(torch.tensor(d["beta_inv"].reshape(-1), dtype=torch.float32, device="cuda"))
+    torch.cuda.synchronize()
+    return torch.cat(feats), torch.cat(targets)
+
+
+def cf_error(cf, cf_ref, mask):
+    return float(np.abs((cf - cf_ref)[mask] / cf_ref[mask]).max())
+
+
+def run(data_dir: str, steps: int = 2000, batch: int = 65536, lr: float = 1e-3, seed: int = 20261203, log=print):
+    import torch
+    from . import inversion as inv
+    paths = sorted(glob.glob(os.path.join(data_dir, "inversion_*.npz")))
+    train_paths = [p for p in paths if HELD_OUT not in os.path.basename(p)]
+    test_paths = [p for p in paths if HELD_OUT in os.path.basename(p)]
+    if not train_paths or not test_paths:
+        raise FileNotFoundError("need the held-out case %s and training cases in %s" % (HELD_OUT, data_dir))
+    out = {"train_cases": [os.path.basename(p) for p in train_paths], "held_out": os.path.basename(test_paths[0])}
+    t0 = time.time()
+    feat, target = training_set(train_paths)
+    f_np = feat.cpu().numpy()
+    mean, std = f_np.mean(axis=0), f_np.std(axis=0) + 1e-6
+    out["samples"] = int(feat.shape[0])
+    out["feature_mean"], out["feature_std"] = mean.tolist(), std.tolist()
+    # train on the held-out case's context (any SA context holds the network)
+    tag, c, d, eq = _eq_for(test_paths[0])
+    eq.mlp_set_normalization(mean, std)
+    eq.mlp_init(seed)
+    torch.cuda.synchronize()
+    t1 = time.time()
+    loss = eq.mlp_train(feat.data_ptr(), target.data_ptr(), int(feat.shape[0]), steps, batch=batch, lr=lr, seed=seed)
+    out["train"] = {"steps": steps, "batch": batch, "lr": lr, "wall_s": time.time() - t1,
+                    "loss_first": float(loss[0]), "loss_last": float(loss[-20:].mean())}
+    log("[train] %s" % out["train"])
+    params = eq.mlp_params()
+    # held-out comparison against the inverted-beta FP64 solution
+    mask = inv.plate_mask(c, d["xv"])
+    cf_inv, cf_target = d["cf_inv"], d["cf_target"]
+    from . import case as C
+
+    def solve(label, beta=None, learned=False):
+        eq.mlp_enable(False)
+        eq.set_beta(np.ones((c.nic, c.njc)) if beta is None else beta)
+        if learned:
+            eq.mlp_enable(True)
+        eq.set_state(C.freestream_state(c))
+        torch.cuda.synchronize()
+        ts = time.time()
+        ok, hist = inv.converge(eq)
+        wall = time.time() - ts
+        cf, J = eq.skin_friction()
+        eq.mlp_enable(False)
+        res = {"converged": bool(ok), "steps": None if hist is None else int(hist.shape[0] - 1), "wall_s": wall,
+               "cf_err_vs_inverted": cf_error(cf, cf_inv, mask), "cf_err_vs_target": cf_error(cf, cf_target, mask),
+               "J": J}
+        log("[%s] %s" % (label, res))
+        return res, cf
+
+    out["plain_sa"], _ = solve("plain SA")
+    out["inverted_beta"], _ = solve("inverted beta", beta=d["beta_inv"])
+    out["learned"], cf_l = solve("learned", learned=True)
+    b = torch.empty(c.nic * c.njc, dtype=torch.float64, device="cuda")
+    eq.mlp_beta_device(b.data_ptr())
+    torch.cuda.synchronize()
+    bl = b.cpu().numpy().reshape(c.nic, c.njc)
+    bl_err = bl - d["beta_inv"]
+    out["learned_beta_rms_err_vs_inverted"] = float(np.sqrt((bl_err ** 2).mean()))
+    out["wall_s"] = time.time() - t0
+    return out, params, loss

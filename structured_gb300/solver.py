@@ -39,6 +39,12 @@ def _vp(x):
     return ctypes.c_void_p(int(x)) if x is not None else None
 
 
+def _f32p(a):
+    if a.dtype != np.float32 or not a.flags.c_contiguous:
+        raise ValueError("arrays must be C-contiguous float32")
+    return ctypes.c_void_p(a.ctypes.data)
+
+
 def load_library() -> ctypes.CDLL:
     """Loads the in-tree CUDA library; raises if it has not been built."""
     global _lib
@@ -84,6 +90,15 @@ def load_library() -> ctypes.CDLL:
         "st_cf_gradient_device": (I, [V, _P, V]),
         "st_adjoint_solve_device": (I, [V, V, V, D, I, I, D, ctypes.POINTER(abi.StSolveStats)]),
         "st_tangent_solve_device": (I, [V, V, V, D, I, I, D, ctypes.POINTER(abi.StSolveStats)]),
+        "st_mlp_param_count": (I, []),
+        "st_mlp_init": (I, [V, ctypes.c_ulonglong]),
+        "st_mlp_set_params": (I, [V, V]),
+        "st_mlp_get_params": (I, [V, V]),
+        "st_mlp_set_normalization": (I, [V, V, V]),
+        "st_mlp_enable": (I, [V, I]),
+        "st_mlp_train": (I, [V, V, V, ctypes.c_long, I, I, ctypes.c_float, ctypes.c_ulonglong, V]),
+        "st_sa_features": (I, [V, V]),
+        "st_mlp_beta": (I, [V, V]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -340,20 +355,57 @@ def _eq_extras():
         w = np.ascontiguousarray(w, dtype=np.float64)
         _check(self.lib.st_cf_gradient_device(self.h, _ptr(w), _vp(grad_ptr)), "st_cf_gradient_device")
 
-    def adjoint_solve_device(self, b_ptr, psi_ptr, cfl_prec=1e6, m=60, maxit=600, rtol=1e-10):
+    def adjoint_solve_device(self, b_ptr, psi_ptr, cfl_prec=1e6, m=150, maxit=4000, rtol=1e-10):
         st = abi.StSolveStats()
         _check(self.lib.st_adjoint_solve_device(self.h, _vp(b_ptr), _vp(psi_ptr), float(cfl_prec), m, maxit,
                                                 float(rtol), ctypes.byref(st)), "st_adjoint_solve_device")
         return st
 
-    def tangent_solve_device(self, b_ptr, dq_ptr, cfl_prec=1e6, m=60, maxit=600, rtol=1e-10):
+    def tangent_solve_device(self, b_ptr, dq_ptr, cfl_prec=1e6, m=150, maxit=4000, rtol=1e-10):
         st = abi.StSolveStats()
         _check(self.lib.st_tangent_solve_device(self.h, _vp(b_ptr), _vp(dq_ptr), float(cfl_prec), m, maxit,
                                                 float(rtol), ctypes.byref(st)), "st_tangent_solve_device")
         return st
 
+    # -- learned SA correction (st_mlp_*) --------------------------------
+    def mlp_init(self, seed: int) -> None:
+        _check(self.lib.st_mlp_init(self.h, int(seed)), "st_mlp_init")
+
+    def mlp_params(self) -> np.ndarray:
+        out = np.empty(self.lib.st_mlp_param_count(), dtype=np.float32)
+        _check(self.lib.st_mlp_get_params(self.h, _f32p(out)), "st_mlp_get_params")
+        return out
+
+    def mlp_set_params(self, params: np.ndarray) -> None:
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        if p.size != self.lib.st_mlp_param_count():
+            raise ValueError("MLP parameter count")
+        _check(self.lib.st_mlp_set_params(self.h, _f32p(p)), "st_mlp_set_params")
+
+    def mlp_set_normalization(self, mean, std) -> None:
+        m = np.ascontiguousarray(mean, dtype=np.float32)
+        sd = np.ascontiguousarray(std, dtype=np.float32)
+        _check(self.lib.st_mlp_set_normalization(self.h, _f32p(m), _f32p(sd)), "st_mlp_set_normalization")
+
+    def mlp_enable(self, on: bool = True) -> None:
+        _check(self.lib.st_mlp_enable(self.h, int(on)), "st_mlp_enable")
+
+    def mlp_train(self, feat_ptr, target_ptr, n: int, steps: int, batch: int = 65536, lr: float = 1e-3,
+                  seed: int = 0) -> np.ndarray:
+        loss = np.zeros(steps, dtype=np.float32)
+        _check(self.lib.st_mlp_train(self.h, _vp(feat_ptr), _vp(target_ptr), int(n), int(steps), int(batch),
+                                     float(lr), int(seed), _f32p(loss)), "st_mlp_train")
+        return loss
+
+    def sa_features_device(self, out_ptr) -> None:
+        _check(self.lib.st_sa_features(self.h, _vp(out_ptr)), "st_sa_features")
+
+    def mlp_beta_device(self, out_ptr) -> None:
+        _check(self.lib.st_mlp_beta(self.h, _vp(out_ptr)), "st_mlp_beta")
+
     for f in (jacobian_assemble, jacobian_blocks, jacobian_apply_device, linear_solve_device, cf_gradient_device,
-              adjoint_solve_device, tangent_solve_device):
+              adjoint_solve_device, tangent_solve_device, mlp_init, mlp_params, mlp_set_params,
+              mlp_set_normalization, mlp_enable, mlp_train, sa_features_device, mlp_beta_device):
         setattr(EulerEquation, f.__name__, f)
 
 
