@@ -340,18 +340,23 @@ def run_ours(args, world, rank, local):
     alg = ALG_BYTES[(tb, "res")] + (ALG_BYTES[(tb, "adj")] if with_adj else 0)
     t_path = adj_ms if with_adj else res_ms
     achieved = alg * cells / (t_path * 1e-3) / 1e9
-    prof = "residual_%s_%s.md" % (tb, args.grid)
+    prof = ("residual_adjoint_%s_%s.md" if with_adj else "residual_%s_%s.md") % (tb, args.grid)
     traffic_cell = profile_figure(prof, "dram_bytes_per_cell")
     flops_cell = profile_figure(prof, "fp64_flops_per_cell")
+    kern = kern_adj if with_adj else kern_res
+    top = max(kern, key=kern.get) if kern else None
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback",
             "traffic": traffic_cell * cells if traffic_cell else None,
             "scope": "whole %s evaluation (%d launches), %d algorithmic B/cell"
                      % ("fused residual+adjoint" if with_adj else "residual", kernels_per_step, alg),
             "kernels_ms": {"residual": kern_res, "adjoint": kern_adj}}
+    if top:
+        roof["dominant_kernel"] = {"name": top, "ms": kern[top], "share": kern[top] / max(sum(kern.values()), 1e-30)}
     if flops_cell:
-        fp64_ach = flops_cell * cells / (res_ms * 1e-3) / 1e12
-        roof["fp64"] = {"scope": "residual pipeline (ncu-counted flops / event time)",
+        fp64_ach = flops_cell * cells / (t_path * 1e-3) / 1e12
+        roof["fp64"] = {"scope": "%s pipeline (ncu-counted flops / event time)"
+                                 % ("fused residual+adjoint" if with_adj else "residual"),
                         "achieved_tflops": fp64_ach, "peak_tflops": fp64_peak, "frac": fp64_ach / fp64_peak,
                         "flops_per_cell": flops_cell, "peak_source": "live DFMA probe (st_probe_fp64)"}
     else:
