@@ -342,7 +342,7 @@ static __global__ void __launch_bounds__(256) k_cell_src(DevCase c, const double
 // the flux adjoint w(R) - w(L), w = psi / V (0 on ghost sides), and, with SA,
 // by the gradient-part adjoints of the two adjacent cells' sources.
 template <int NQ, int DIR, int ORDER>
-__global__ void __launch_bounds__(256) k_face_fused(DevCase c, const double* __restrict__ P,
+__global__ void __launch_bounds__(256, 2) k_face_fused(DevCase c, const double* __restrict__ P,
                                                     const double* __restrict__ lim, const double* __restrict__ psi,
                                                     const double* __restrict__ srec, double* __restrict__ F,
                                                     double* __restrict__ arec) {

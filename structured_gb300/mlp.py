@@ -7,7 +7,9 @@ module is new.
 
 DIR holds the inversion_<tag>_<ni>x<nj>.npz files the inversion run writes.
 Training pairs are (features of the inverted state, inverted beta) over all
-cells of the eight cases other than Re_L = 3e6 at -2 degrees.
+cells of the cases other than Re_L = 3e6 at -2 degrees whose inversion matched
+its target (plate Cf within `max_cf_err`, 5 %): an inversion that stalled far
+from its target leaves a beta field that contradicts the others.
 """
 from __future__ import annotations
 
@@ -58,15 +60,26 @@ def cf_error(cf, cf_ref, mask):
     return float(np.abs((cf - cf_ref)[mask] / cf_ref[mask]).max())
 
 
-def run(data_dir: str, steps: int = 2000, batch: int = 65536, lr: float = 1e-3, seed: int = 20261203, log=print):
+def inversion_cf_error(path: str) -> float:
+    from . import inversion as inv
+    _, c = _case_of(path)
+    d = np.load(path)
+    return cf_error(d["cf_inv"], d["cf_target"], inv.plate_mask(c, d["xv"]))
+
+
+def run(data_dir: str, steps: int = 2000, batch: int = 65536, lr: float = 1e-3, seed: int = 20261203,
+        max_cf_err: float = 0.05, log=print):
     import torch
     from . import inversion as inv
     paths = sorted(glob.glob(os.path.join(data_dir, "inversion_*.npz")))
-    train_paths = [p for p in paths if HELD_OUT not in os.path.basename(p)]
     test_paths = [p for p in paths if HELD_OUT in os.path.basename(p)]
+    others = [p for p in paths if HELD_OUT not in os.path.basename(p)]
+    errs = {os.path.basename(p): inversion_cf_error(p) for p in others}
+    train_paths = [p for p in others if errs[os.path.basename(p)] <= max_cf_err]
     if not train_paths or not test_paths:
         raise FileNotFoundError("need the held-out case %s and training cases in %s" % (HELD_OUT, data_dir))
-    out = {"train_cases": [os.path.basename(p) for p in train_paths], "held_out": os.path.basename(test_paths[0])}
+    out = {"train_cases": [os.path.basename(p) for p in train_paths], "held_out": os.path.basename(test_paths[0]),
+           "excluded": {k: v for k, v in errs.items() if v > max_cf_err}}
     t0 = time.time()
     feat, target = training_set(train_paths)
     f_np = feat.cpu().numpy()
