@@ -141,6 +141,11 @@ int st_norms(st_ctx* ctx, double* out);
  * src/utils/io.cpp:217-226), of the current state; cf_host [nic].  J is
  * sum Cf dx over plate faces with x <= plate_x_end. */
 int st_skin_friction(st_ctx* ctx, double* cf_host, double* J);
+/* Velocity gradients (u_x, u_y, v_x, v_y) of the current state at the j = 0
+ * faces, [nic][4] on the host: the row of the reference's grad_u_eta /
+ * grad_v_eta that IOManager::write_surface reads for Cf and the viscous
+ * Cl/Cd (src/utils/io.cpp:217-236). */
+int st_wall_gradients(st_ctx* ctx, double* out_host);
 
 /* Forward-mode Jacobian-vector product (dR/dQ) v + (dR/dbeta) vb on the
  * context state; vb may be NULL.  Replaces one column sweep of ADOL-C's
@@ -191,6 +196,16 @@ int st_solve(st_ctx* ctx, const st_solve_params* params, st_solve_stats* stats, 
              int history_len, int* steps_done);
 /* grad_dev = d(sum_i w_i Cf_i)/dQ at the context state for wall weights
  * w_host[nic] (drag: w = dx; inversion misfit: w = 2 (Cf - Cf*)). */
+/* Explicit marching of Solver::step's explicit branch (src/solver/solver.cpp:
+ * 103-116): scheme 0 = forward_euler (q += R dt), 1 = rk4_jameson (stages
+ * q_s = q + R(q_{s-1}) dt / (4 - s), s = 0..3, q_{-1} = q), dt from calc_dt
+ * at each step's start (every component; the reference leaves the transport
+ * slot unset).  Norms of the last stage's residual, as the reference logs
+ * them, every `check_every` steps into history ([step, norms...]); stops at
+ * max_k ||R_k|| <= tolerance (0: run all steps; ST_ERR_NOCONV if a positive
+ * tolerance is not reached).  Periodic and wake boundaries are supported. */
+int st_explicit_solve(st_ctx* ctx, int scheme, double cfl, int steps, double tolerance, int check_every,
+                      double* history, int history_len, int* steps_done);
 int st_cf_gradient_device(st_ctx* ctx, const double* w_host, double* grad_dev);
 /* Adjoint solve (dR/dQ)^T psi = b with the exact Jacobian of the residual;
  * the preconditioner adds I/dt(cfl_prec).  psi holds the initial guess. */

@@ -144,4 +144,17 @@ int refh_eta_gradients(void* h, double* out) {
     return 0;
 }
 
+/* IOManager::write (src/utils/io.cpp:41-47) on state q: the reference writes
+ * <io.label>.tec, .npz, .out and .surface.  The residual of q is evaluated
+ * first (as Solver::step has done before it writes) so the wall-face
+ * gradients the surface file reads belong to q. */
+int refh_write_outputs(void* h, const double* q) {
+    auto* rc = static_cast<RefCase*>(h);
+    auto sol = rc->mesh->solution;
+    std::memcpy(sol->q.data(), q, sol->q.size() * sizeof(double));
+    rc->mesh->equation->calc_residual(sol->q.const_ref(), sol->rhs);
+    rc->mesh->iomanager->write(0);
+    return 0;
+}
+
 }  // extern "C"

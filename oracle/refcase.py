@@ -44,6 +44,7 @@ def load(kind: str = "serial") -> ctypes.CDLL:
     lib.refh_metrics.argtypes = [ctypes.c_void_p, _P, _P, _P]
     lib.refh_primitives.argtypes = [ctypes.c_void_p, _P]
     lib.refh_eta_gradients.argtypes = [ctypes.c_void_p, _P]
+    lib.refh_write_outputs.argtypes = [ctypes.c_void_p, _P]
     _libs[kind] = lib
     return lib
 
@@ -110,3 +111,8 @@ class RefCase:
         out = np.empty((self.nic, self.nj, 4))
         self.lib.refh_eta_gradients(self.h, _ptr(out))
         return out
+
+    def write_outputs(self, q: np.ndarray) -> None:
+        """The reference's IOManager::write of state q (files under the case's io.label)."""
+        q = np.ascontiguousarray(q, dtype=np.float64)
+        self.lib.refh_write_outputs(self.h, _ptr(q))

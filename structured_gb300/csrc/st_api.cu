@@ -249,6 +249,26 @@ __global__ void k_skin_friction(DevCase c, const double* __restrict__ P, double 
     cf[i] = c.mu_inf * (uy - vx) / qinf;
 }
 
+// velocity gradients (u_x, u_y, v_x, v_y) at the j = 0 faces, the row of
+// grad_u_eta / grad_v_eta that IOManager::write_surface reads
+// (src/utils/io.cpp:217-236), with the face-gradient weights of k_skin_friction
+__global__ void k_wall_gradients(DevCase c, const double* __restrict__ P, double* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c.nic) return;
+    const FaceIdx fi = face_idx<1>(c, i, 0);
+    const double* gm = c.geo_j + fi.face * NGEO;
+    const double* pL = P + fi.L; const double* pR = P + fi.R;
+    const double* a = P + fi.Pa; const double* b = P + fi.Pb;
+    const double* m = P + fi.Ma; const double* n = P + fi.Mb;
+    double* o = out + (size_t)i * 4;
+#pragma unroll
+    for (int s = 0; s < 2; s++) {
+        const int f = s == 0 ? P_U : P_V;
+        o[2 * s + 0] = gm[G_WLX] * pL[f] + gm[G_WRX] * pR[f] + gm[G_WPX] * (a[f] + b[f]) + gm[G_WMX] * (m[f] + n[f]);
+        o[2 * s + 1] = gm[G_WLY] * pL[f] + gm[G_WRY] * pR[f] + gm[G_WPY] * (a[f] + b[f]) + gm[G_WMY] * (m[f] + n[f]);
+    }
+}
+
 __global__ void k_fill(double* a, size_t n, double v) {
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) a[i] = v;
 }
@@ -531,7 +551,8 @@ int st_destroy(st_ctx* x) {
     double* bufs[] = {x->q, x->rhs, x->beta, x->P, x->lim, x->Fi, x->Fj, x->Gi, x->Gj, x->vol_d, x->ivol_d,
                       x->geo_i, x->geo_j, x->wd, x->nchi_d, x->neta_d, x->dsmin_d, x->dt, x->norm_part, x->norm_out,
                       x->cf, x->wall_dx_d, x->Pbar, x->srec, x->arec_i, x->arec_j, x->psi_tmp,
-                      x->outq_tmp, x->outb_tmp, x->tape, x->jac, x->jac1, x->kv, x->kzb, x->kz, x->kw, x->kr, x->kh, x->kpart, x->dq, x->qsave};
+                      x->outq_tmp, x->outb_tmp, x->tape, x->jac, x->jac1, x->kv, x->kzb, x->kz, x->kw, x->kr, x->kh, x->kpart, x->dq, x->qsave,
+                      x->qtmp};
     for (double* b : bufs) if (b) cudaFree(b);
     st::dual* dbufs[] = {x->qd, x->Pd, x->limd, x->Fdi, x->Fdj, x->Gdi, x->Gdj, x->rhsd, x->betad};
     for (st::dual* b : dbufs) if (b) cudaFree(b);
@@ -652,6 +673,27 @@ int st_skin_friction(st_ctx* x, double* cf_host, double* J) {
     for (size_t i = 0; i < cf.size(); i++) s += cf[i] * x->wall_dx[i];
     if (cf_host) std::memcpy(cf_host, cf.data(), cf.size() * 8);
     if (J) *J = s;
+    return ST_OK;
+}
+
+int st_wall_gradients(st_ctx* x, double* out_host) {
+    if (!x || !out_host) return fail(ST_ERR_ARG, "st_wall_gradients: null argument");
+    const DevCase& dc = x->dc;
+    if (x->nq == 5) {
+        k_prim<double, 5><<<grid_for(x->ncell), 256, 0, x->stream>>>(dc, x->q, x->P);
+        k_bc<double, 5><<<1, 1024, 0, x->stream>>>(dc, x->P);
+    } else {
+        k_prim<double, 4><<<grid_for(x->ncell), 256, 0, x->stream>>>(dc, x->q, x->P);
+        k_bc<double, 4><<<1, 1024, 0, x->stream>>>(dc, x->P);
+    }
+    const int nic = x->c.ni - 1;
+    double* d = nullptr;
+    ST_CUDA(cudaMallocAsync((void**)&d, (size_t)nic * 4 * 8, x->stream));
+    k_wall_gradients<<<grid_for(nic), 256, 0, x->stream>>>(dc, x->P, d);
+    ST_LAUNCH_CHECK("wall gradients");
+    ST_CUDA(cudaMemcpyAsync(out_host, d, (size_t)nic * 4 * 8, cudaMemcpyDeviceToHost, x->stream));
+    ST_CUDA(cudaFreeAsync(d, x->stream));
+    ST_CUDA(cudaStreamSynchronize(x->stream));
     return ST_OK;
 }
 

@@ -39,6 +39,7 @@ struct st_ctx {
     double *jac = nullptr, *jac1 = nullptr, *kv = nullptr, *kz = nullptr, *kw = nullptr, *kr = nullptr;
     double *kh = nullptr, *kpart = nullptr, *dq = nullptr, *qsave = nullptr;
     double* kzb = nullptr;   // flexible GMRES: preconditioned basis Z = M^{-1} V
+    double* qtmp = nullptr;  // explicit RK stage state (Solution::q_tmp)
     float* lfac = nullptr;   // block ILU(0) factors, FP32: [cell][9][nq][nq]
     // learned SA correction: BF16 weights, FP32 biases + normalisation, FP32
     // master parameters with Adam moments, training partials

@@ -560,6 +560,13 @@ __global__ void k_combine(const double* __restrict__ V, int nvec, size_t n, cons
         y[t] = s;
     }
 }
+// explicit stage, the arithmetic of update_forward_euler / update_rk4
+// (src/solver/solver.cpp:12-26): out = q + rhs * dt / denom
+__global__ void k_stage(size_t n, const double* q, const double* __restrict__ rhs,
+                        const double* __restrict__ dt, double denom, double* out) {
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x)
+        out[t] = q[t] + rhs[t] * dt[t] / denom;
+}
 __global__ void k_axpby(size_t n, double a, const double* __restrict__ x, double b, double* __restrict__ y) {
     for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x)
         y[t] = a * x[t] + b * y[t];
@@ -1018,6 +1025,58 @@ int st_solve(st_ctx* x, const st_solve_params* p, st_solve_stats* stats, double*
     if (stats) *stats = ls;
     if (steps_done) *steps_done = accepted;
     if (!converged) return fail(ST_ERR_NOCONV, "st_solve: tolerance not reached");
+    return ST_OK;
+}
+
+int st_explicit_solve(st_ctx* x, int scheme, double cfl, int steps, double tolerance, int check_every,
+                      double* history, int history_len, int* steps_done) {
+    if (!x) return fail(ST_ERR_ARG, "st_explicit_solve: null context");
+    if ((scheme != 0 && scheme != 1) || !(cfl > 0.0) || steps < 0 || check_every < 1)
+        return fail(ST_ERR_ARG, "st_explicit_solve: scheme 0 (forward_euler) or 1 (rk4_jameson), cfl > 0, check_every >= 1");
+    const int nq = x->nq;
+    const size_t n = x->ncell * nq;
+    const unsigned g = grid_for(n);
+    cudaStream_t s = x->stream;
+    if (scheme == 1 && !x->qtmp) {
+        if (cudaMalloc((void**)&x->qtmp, n * 8) != cudaSuccess) return fail(ST_ERR_CUDA, "cudaMalloc (RK stage state)");
+    }
+    std::vector<double> nrm(nq);
+    int hist = 0, done = 0;
+    bool converged = false;
+    for (done = 0; done < steps;) {
+        int rc = stx::run_dt(x, cfl);  // EulerEquation::calc_dt at the step's start (solver.cpp:66)
+        if (rc) return rc;
+        if (scheme == 0) {
+            rc = stx::run_residual(x, x->q, x->beta, x->rhs, x->c.order);
+            if (rc) return rc;
+            k_stage<<<g, 256, 0, s>>>(n, x->q, x->rhs, x->dt, 1.0, x->q);
+        } else {
+            ST_CUDA(cudaMemcpyAsync(x->qtmp, x->q, n * 8, cudaMemcpyDeviceToDevice, s));
+            for (int st = 0; st < 4; st++) {
+                rc = stx::run_residual(x, x->qtmp, x->beta, x->rhs, x->c.order);
+                if (rc) return rc;
+                k_stage<<<g, 256, 0, s>>>(n, x->q, x->rhs, x->dt, 4.0 - st, x->qtmp);
+            }
+            ST_CUDA(cudaMemcpyAsync(x->q, x->qtmp, n * 8, cudaMemcpyDeviceToDevice, s));
+        }
+        ST_LAUNCH_CHECK("explicit step");
+        x->have_residual = false;
+        done++;
+        if (done % check_every == 0 || done == steps) {
+            rc = stx::run_norms(x, x->rhs, nrm.data());
+            if (rc) return rc;
+            if (history && hist + nq + 1 <= history_len) {
+                history[hist++] = done;
+                for (int k = 0; k < nq; k++) history[hist++] = nrm[k];
+            }
+            double m = 0.0;
+            for (int k = 0; k < nq; k++) m = std::max(m, nrm[k]);
+            if (tolerance > 0.0 && m <= tolerance) { converged = true; break; }
+        }
+    }
+    ST_CUDA(cudaStreamSynchronize(s));
+    if (steps_done) *steps_done = done;
+    if (tolerance > 0.0 && !converged) return fail(ST_ERR_NOCONV, "st_explicit_solve: tolerance not reached");
     return ST_OK;
 }
 

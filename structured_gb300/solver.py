@@ -90,6 +90,8 @@ def load_library() -> ctypes.CDLL:
         "st_cf_gradient_device": (I, [V, _P, V]),
         "st_adjoint_solve_device": (I, [V, V, V, D, I, I, D, ctypes.POINTER(abi.StSolveStats)]),
         "st_tangent_solve_device": (I, [V, V, V, D, I, I, D, ctypes.POINTER(abi.StSolveStats)]),
+        "st_explicit_solve": (I, [V, I, D, I, D, I, V, I, ctypes.POINTER(I)]),
+        "st_wall_gradients": (I, [V, V]),
         "st_mlp_param_count": (I, []),
         "st_mlp_init": (I, [V, ctypes.c_ulonglong]),
         "st_mlp_set_params": (I, [V, V]),
@@ -367,6 +369,27 @@ def _eq_extras():
                                                 float(rtol), ctypes.byref(st)), "st_tangent_solve_device")
         return st
 
+    def explicit_solve(self, scheme: str = "rk4_jameson", cfl: float | None = None, steps: int = 1000,
+                       tolerance: float = 0.0, check_every: int = 100, raise_on_noconv: bool = True):
+        """Explicit marching (Solver::step's forward_euler / rk4_jameson);
+        returns (steps done, history rows [step, norms...])."""
+        code = {"forward_euler": 0, "rk4_jameson": 1}[scheme]
+        cfl = self.case.cfl if cfl is None else cfl
+        hist = np.zeros((steps // check_every + 2) * (1 + self.nq))
+        done = ctypes.c_int()
+        rc = self.lib.st_explicit_solve(self.h, code, float(cfl), int(steps), float(tolerance), int(check_every),
+                                        _ptr(hist), hist.size, ctypes.byref(done))
+        if rc and not (rc == -4 and not raise_on_noconv):
+            _check(rc, "st_explicit_solve")
+        rows = hist.reshape(-1, 1 + self.nq)
+        return done.value, rows[rows[:, 0] > 0]
+
+    def wall_gradients(self) -> np.ndarray:
+        """(u_x, u_y, v_x, v_y) at the j = 0 faces of the current state, [nic][4]."""
+        out = np.empty((self.nic, 4))
+        _check(self.lib.st_wall_gradients(self.h, _ptr(out)), "st_wall_gradients")
+        return out
+
     # -- learned SA correction (st_mlp_*) --------------------------------
     def mlp_init(self, seed: int) -> None:
         _check(self.lib.st_mlp_init(self.h, int(seed)), "st_mlp_init")
@@ -404,7 +427,7 @@ def _eq_extras():
         _check(self.lib.st_mlp_beta(self.h, _vp(out_ptr)), "st_mlp_beta")
 
     for f in (jacobian_assemble, jacobian_blocks, jacobian_apply_device, linear_solve_device, cf_gradient_device,
-              adjoint_solve_device, tangent_solve_device, mlp_init, mlp_params, mlp_set_params,
+              adjoint_solve_device, tangent_solve_device, explicit_solve, wall_gradients, mlp_init, mlp_params, mlp_set_params,
               mlp_set_normalization, mlp_enable, mlp_train, sa_features_device, mlp_beta_device):
         setattr(EulerEquation, f.__name__, f)
 

@@ -6,7 +6,8 @@ Run from the repository root where the reference sources are mounted:
     make -C oracle ref port && python tests/golden/make_golden.py
 Each fixture stores the grid, the case, a seeded state and the reference's
 calc_residual (both reconstruction orders), calc_dt and ghost-padded
-primitives, plus the per-cell flux scale used to state relative errors.
+primitives, plus the per-cell flux scale used to state relative errors;
+io_fp.npz holds the reference's output files for one state.
 """
 from __future__ import annotations
 
@@ -41,8 +42,36 @@ def cases(tmp: str):
     yield "inviscid", c, 19
 
 
+def io_fixture(tmp: str):
+    """The reference's own output files (IOManager::write, src/utils/io.cpp:41-255)
+    for one flat-plate state: tecplot, npz, restart and surface text, with the
+    wall-face gradients and primitives the surface file was computed from."""
+    c = C.flat_plate_case(tmp, "io_fp", 41, 21, 0.3, 1e6, 1e-4, 1.08, lhs_order=1)
+    c.tail = 1  # surface faces [tail-1, ni-tail): the whole bottom row
+    C.write_inp(os.path.join(tmp, "io_fp.inp"), c)
+    xv, yv = C.load_grid(c)
+    q = C.perturbed_state(c, 23)
+    ref = RefCase(os.path.join(tmp, "io_fp.inp"))
+    ref.write_outputs(q)
+    lab = c.label
+    ref_npz = np.load(lab + ".npz")
+    d = C.case_to_dict(c)
+    d["grid_path"] = ""
+    d["label"] = "io_fp"
+    with open(lab + ".surface") as f:
+        surface = f.read()
+    with open(lab + ".tec") as f:
+        tec = f.read()
+    out = np.fromfile(lab + ".out", dtype=np.uint8)
+    np.savez_compressed(os.path.join(OUT, "io_fp.npz"), case=json.dumps(d), xv=xv, yv=yv, q=q,
+                        surface=surface, tec=tec, out=out, wall_grad=ref.eta_gradients()[:, 0, :],
+                        **{"npz_" + k: ref_npz[k] for k in ref_npz.files})
+    print("io_fp", q.shape, len(surface.splitlines()), "surface lines")
+
+
 def main():
     with tempfile.TemporaryDirectory() as tmp:
+        io_fixture(tmp)
         for name, c, seed in cases(tmp):
             xv, yv = C.load_grid(c)
             ref = RefCase(os.path.join(tmp, name + ".inp"))
