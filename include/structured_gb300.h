@@ -43,6 +43,8 @@ enum { ST_BC_FREESTREAM = 0, ST_BC_SLIPWALL = 1, ST_BC_WALL = 2, ST_BC_OUTFLOW =
 enum { ST_FACE_BOTTOM = 0, ST_FACE_RIGHT = 1, ST_FACE_TOP = 2, ST_FACE_LEFT = 3 };
 enum { ST_VISC_POWER = 0, ST_VISC_SUTHERLAND = 1 };
 enum { ST_TURB_NONE = 0, ST_TURB_SA = 1 };
+/* [solver] flux: Roe (flux.cpp:51-146) or AUSM (flux.cpp:148-224, the reference's default) */
+enum { ST_FLUX_ROE = 0, ST_FLUX_AUSM = 1 };
 
 /* One [[boundary]] table.  start/end are ghost-padded indices along the face;
  * a negative end counts from the end as in BoundaryContainer::get_index
@@ -61,6 +63,7 @@ typedef struct st_case {
     int32_t turbulence;             /* ST_TURB_* */
     int32_t nbc;
     int32_t plate_vertex;           /* first no-slip wall vertex (objective) */
+    int32_t flux;                   /* ST_FLUX_*; the hand-written adjoint reverses Roe only */
     double rho_inf, u_inf, v_inf, p_inf, T_inf, mu_inf, pr_inf;
     double dpdx, dpdy;              /* [source] body force */
     double nu_tilde_inf;            /* SA freestream nu_tilde */

@@ -535,6 +535,61 @@ void roe_flux(const PCase& pc, const double* normal, int nfaces,
     }
 }
 
+// ConvectiveFluxAUSM::evaluate, src/model/flux.cpp:148-224, in its operation
+// order (split Mach numbers / pressures of flux.cpp:148-155).
+template <class T> T ausm_mach_p(const T& M) { return fabs(M) <= 1.0 ? 0.25 * (M + 1.0) * (M + 1.0) : 0.5 * (M + fabs(M)); }
+template <class T> T ausm_mach_m(const T& M) { return fabs(M) <= 1.0 ? -0.25 * (M - 1.0) * (M - 1.0) : 0.5 * (M - fabs(M)); }
+template <class T> T ausm_pres_p(const T& M, const T& p) {
+    return fabs(M) <= 1.0 ? 0.25 * p * (M + 1.0) * (M + 1.0) * (2.0 - M) : 0.5 * p * (M + fabs(M)) / M;
+}
+template <class T> T ausm_pres_m(const T& M, const T& p) {
+    return fabs(M) <= 1.0 ? 0.25 * p * (M - 1.0) * (M - 1.0) * (2.0 + M) : 0.5 * p * (M - fabs(M)) / M;
+}
+
+template <class T>
+void ausm_flux(const PCase& pc, const double* normal, int nfaces,
+               const std::vector<T>* L, const std::vector<T>* Rr, std::vector<T>& f) {
+    constexpr double gm1 = GAMMA - 1.0;
+    constexpr double ogm1 = 1.0 / gm1;
+    const int nq = pc.nq;
+#pragma omp parallel for schedule(static)
+    for (int idx = 0; idx < nfaces; idx++) {
+        const double nx = normal[idx * 2 + 0], ny = normal[idx * 2 + 1];
+        const T rlft = L[0][idx], ulft = L[1][idx], vlft = L[2][idx], plft = L[3][idx];
+        const T rrht = Rr[0][idx], urht = Rr[1][idx], vrht = Rr[2][idx], prht = Rr[3][idx];
+        const double ds = std::sqrt(nx * nx + ny * ny);
+        const T ulft_normal = (ulft * nx + vlft * ny) / ds;
+        const T urht_normal = (urht * nx + vrht * ny) / ds;
+        const T alft = sqrt(GAMMA * plft / rlft);
+        const T arht = sqrt(GAMMA * prht / rrht);
+        const T machlft = ulft_normal / alft;
+        const T machrht = urht_normal / arht;
+        const T rlfti = 1.0 / rlft;
+        const T uvl = 0.5 * (ulft * ulft + vlft * vlft);
+        const T elft = plft * ogm1 + rlft * uvl;
+        const T hlft = (elft + plft) * rlfti;
+        const T rrhti = 1.0 / rrht;
+        const T uvr = 0.5 * (urht * urht + vrht * vrht);
+        const T erht = prht * ogm1 + rrht * uvr;
+        const T hrht = (erht + prht) * rrhti;
+        const T mach_half = ausm_mach_p(machlft) + ausm_mach_m(machrht);
+        const T p_half = ausm_pres_p(machlft, plft) + ausm_pres_m(machrht, prht);
+        T* o = &f[(size_t)idx * nq];
+        if (mach_half >= 0.0) {
+            o[0] = rlft * alft * mach_half * ds;
+            o[1] = rlft * alft * ulft * mach_half * ds + p_half * nx;
+            o[2] = rlft * alft * vlft * mach_half * ds + p_half * ny;
+            o[3] = rlft * alft * hlft * mach_half * ds;
+        } else {
+            o[0] = rrht * arht * mach_half * ds;
+            o[1] = rrht * arht * urht * mach_half * ds + p_half * nx;
+            o[2] = rrht * arht * vrht * mach_half * ds + p_half * ny;
+            o[3] = rrht * arht * hrht * mach_half * ds;
+        }
+        if (nq == 5) o[4] = o[0] * (o[0] >= 0.0 ? L[4][idx] : Rr[4][idx]);
+    }
+}
+
 // DiffusiveFluxGreenGauss::evaluate, src/model/flux.cpp:12-48 (+ SA diffusion
 // (1/sigma)(mu + rho nu_tilde) grad(nu_tilde) . n in slot 4).
 template <class T>
@@ -633,8 +688,13 @@ void residual(const PCase& pc, const T* q, const T* beta, T* rhs, int order, Wor
 
     for (size_t n = 0; n < (size_t)nic * njc * nq; n++) rhs[n] = 0.0;
     if (scale) for (size_t n = 0; n < (size_t)nic * njc * nq; n++) scale[n] = 0.0;
-    roe_flux(pc, pc.nchi.data(), ni * njc, w.lchi, w.rchi, w.fchi);
-    roe_flux(pc, pc.neta.data(), nic * nj, w.leta, w.reta, w.feta);
+    if (pc.c.flux == ST_FLUX_AUSM) {  // EulerEquation's flux choice, eulerequation.cpp:121-128
+        ausm_flux(pc, pc.nchi.data(), ni * njc, w.lchi, w.rchi, w.fchi);
+        ausm_flux(pc, pc.neta.data(), nic * nj, w.leta, w.reta, w.feta);
+    } else {
+        roe_flux(pc, pc.nchi.data(), ni * njc, w.lchi, w.rchi, w.fchi);
+        roe_flux(pc, pc.neta.data(), nic * nj, w.leta, w.reta, w.feta);
+    }
 #pragma omp parallel for schedule(static)
     for (int i = 0; i < nic; i++)
         for (int j = 0; j < njc; j++)

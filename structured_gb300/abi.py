@@ -17,6 +17,7 @@ BC_TYPES = {"freestream": 0, "slipwall": 1, "wall": 2, "outflow": 3, "periodic":
 FACES = {"bottom": 0, "right": 1, "top": 2, "left": 3}
 VISC = {"power": 0, "sutherland": 1}
 TURB = {"none": 0, "sa": 1}
+FLUX = {"roe": 0, "ausm": 1}
 
 
 class StBc(ctypes.Structure):
@@ -29,7 +30,7 @@ class StCase(ctypes.Structure):
     _fields_ = [("ni", ctypes.c_int32), ("nj", ctypes.c_int32), ("order", ctypes.c_int32),
                 ("lhs_order", ctypes.c_int32), ("viscosity_law", ctypes.c_int32),
                 ("turbulence", ctypes.c_int32), ("nbc", ctypes.c_int32),
-                ("plate_vertex", ctypes.c_int32),
+                ("plate_vertex", ctypes.c_int32), ("flux", ctypes.c_int32),
                 ("rho_inf", ctypes.c_double), ("u_inf", ctypes.c_double), ("v_inf", ctypes.c_double),
                 ("p_inf", ctypes.c_double), ("T_inf", ctypes.c_double), ("mu_inf", ctypes.c_double),
                 ("pr_inf", ctypes.c_double), ("dpdx", ctypes.c_double), ("dpdy", ctypes.c_double),
@@ -57,6 +58,9 @@ def make_case_struct(c: "_case.Case"):
     s.lhs_order = c.lhs_order if c.lhs_order is not None else c.order
     s.viscosity_law = VISC[c.viscosity_law]
     s.turbulence = TURB[c.turbulence]
+    if c.flux not in FLUX:
+        raise ValueError("flux %r: roe or ausm" % c.flux)
+    s.flux = FLUX[c.flux]
     s.nbc = len(c.boundaries)
     s.plate_vertex = c.i_le
     s.rho_inf, s.u_inf, s.v_inf = c.rho_inf, c.u_inf, c.v_inf

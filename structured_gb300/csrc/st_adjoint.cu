@@ -87,6 +87,8 @@ int fused_launches(const st_ctx* x, int order, bool with_rhs) {
 }
 
 int run_fused(st_ctx* x, const double* psi, double* rhs, double* outq, double* outb, int lhs) {
+    if (x->c.flux != ST_FLUX_ROE)
+        return stx::fail(ST_ERR_UNSUPPORTED, "adjoint: the hand-written reverse covers the Roe flux only");
     int rc = ensure(x);
     if (rc) return rc;
     const int order = lhs ? x->c.lhs_order : x->c.order;

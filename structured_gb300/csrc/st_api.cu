@@ -420,6 +420,7 @@ int st_create(const st_case* c, const double* xv, const double* yv, int device, 
     if (c->nbc < 0 || (c->nbc > 0 && !c->bcs)) return fail(ST_ERR_ARG, "st_create: bad boundary list");
     if (c->turbulence != ST_TURB_NONE && c->turbulence != ST_TURB_SA) return fail(ST_ERR_ARG, "st_create: turbulence");
     if (c->viscosity_law != ST_VISC_POWER && c->viscosity_law != ST_VISC_SUTHERLAND) return fail(ST_ERR_ARG, "st_create: viscosity_law");
+    if (c->flux != ST_FLUX_ROE && c->flux != ST_FLUX_AUSM) return fail(ST_ERR_ARG, "st_create: flux");
     for (int b = 0; b < c->nbc; b++) {
         const st_bc& bc = c->bcs[b];
         if (bc.type < 0 || bc.type > ST_BC_WAKE || bc.face < 0 || bc.face > 3)
@@ -526,6 +527,7 @@ int st_create(const st_case* c, const double* xv, const double* yv, int device, 
     dc.viscous = c->mu_inf > 1e-15;  // src/utils/config.cpp:41
     dc.sa = (c->turbulence == ST_TURB_SA);
     dc.law = c->viscosity_law;
+    dc.flux = c->flux;
     dc.nbc = c->nbc;
     dc.R = c->p_inf / c->rho_inf / c->T_inf;  // src/model/fluid.cpp:12
     dc.cp = GAMMA * dc.R / (GAMMA - 1.0);

@@ -19,6 +19,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "../../include/structured_gb300.h"
+
 namespace st {
 
 constexpr double GAMMA = 1.4;
@@ -50,6 +52,7 @@ struct DevBC {
 struct DevCase {
     int ni, nj, nic, njc, nq;
     int viscous, sa, law, nbc;
+    int flux;              // ST_FLUX_ROE / ST_FLUX_AUSM
     double R, cp, pr, rho_inf, u_inf, v_inf, p_inf, T_inf, mu_inf, nut_inf;
     double suth_S, eps_chi, eps_eta, dpdx, dpdy;
     const double* vol;     // [nic][njc]

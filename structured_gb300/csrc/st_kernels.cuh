@@ -227,6 +227,43 @@ __global__ void __launch_bounds__(256) k_limiter(DevCase c, const T* __restrict_
 }
 
 // ----------------------------------------------------------------------------
+// AUSM flux, ConvectiveFluxAUSM::evaluate (src/model/flux.cpp:148-224): split
+// Mach numbers and pressures (van Leer polynomials for |M| <= 1), upwinded by
+// the sign of the interface Mach number; nx, ny the face normal scaled by its
+// length ds.
+// ----------------------------------------------------------------------------
+template <class T>
+__device__ inline T ausm_mach(T M, double s) {  // s = +1: M+, s = -1: M-
+    if (val(tfabs(M)) <= 1.0) return (0.25 * s) * (M + s) * (M + s);
+    return 0.5 * (M + s * tfabs(M));
+}
+template <class T>
+__device__ inline T ausm_pres(T M, T p, double s) {
+    if (val(tfabs(M)) <= 1.0) return 0.25 * p * (M + s) * (M + s) * (2.0 - s * M);
+    return 0.5 * p * (M + s * tfabs(M)) * rcp(M);
+}
+template <class T>
+__device__ inline void ausm_flux(T rlft, T ulft, T vlft, T plft, T rrht, T urht, T vrht, T prht, double nx, double ny,
+                                 double ds, T* f) {
+    const double ids = 1.0 / ds;
+    const T alft = tsqrt(GAMMA * plft * rcp(rlft));
+    const T arht = tsqrt(GAMMA * prht * rcp(rrht));
+    const T mlft = (ulft * nx + vlft * ny) * ids * rcp(alft);
+    const T mrht = (urht * nx + vrht * ny) * ids * rcp(arht);
+    const T mhalf = ausm_mach(mlft, 1.0) + ausm_mach(mrht, -1.0);
+    const T phalf = ausm_pres(mlft, plft, 1.0) + ausm_pres(mrht, prht, -1.0);
+    const bool left = val(mhalf) >= 0.0;
+    const T r = left ? rlft : rrht, a = left ? alft : arht, u = left ? ulft : urht, v = left ? vlft : vrht;
+    const T p = left ? plft : prht;
+    const T h = (p * OGM1 + r * (0.5 * (u * u + v * v)) + p) * rcp(r);
+    const T m = r * a * mhalf * ds;
+    f[0] = m;
+    f[1] = m * u + phalf * nx;
+    f[2] = m * v + phalf * ny;
+    f[3] = m * h;
+}
+
+// ----------------------------------------------------------------------------
 // Roe flux, ConvectiveFluxRoe::evaluate (src/model/flux.cpp:51-146), with the
 // face's unit normal and half length precomputed.
 // ----------------------------------------------------------------------------
@@ -357,7 +394,10 @@ __global__ void __launch_bounds__(256) k_face(DevCase c, const T* __restrict__ P
             }
         }
         T f[NQ];
-        roe_flux(qL[0], qL[1], qL[2], qL[3], qR[0], qR[1], qR[2], qR[3], gm[G_R1], gm[G_R2], gm[G_AJ], f);
+        if (c.flux == ST_FLUX_AUSM)
+            ausm_flux(qL[0], qL[1], qL[2], qL[3], qR[0], qR[1], qR[2], qR[3], gm[G_NX], gm[G_NY], 2.0 * gm[G_AJ], f);
+        else
+            roe_flux(qL[0], qL[1], qL[2], qL[3], qR[0], qR[1], qR[2], qR[3], gm[G_R1], gm[G_R2], gm[G_AJ], f);
         if (NQ == 5) f[4] = f[0] * (val(f[0]) >= 0.0 ? qL[4] : qR[4]);
         if (c.viscous) {
             const T* pPa = P + fi.Pa; const T* pPb = P + fi.Pb;

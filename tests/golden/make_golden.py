@@ -40,6 +40,19 @@ def cases(tmp: str):
                     C.Boundary("freestream", "left", 0, -1), C.Boundary("outflow", "right", 0, -1)]
     C.write_inp(os.path.join(tmp, "inviscid.inp"), c)
     yield "inviscid", c, 19
+    # AUSM (the reference's default flux): subsonic viscous plate, and a supersonic
+    # inviscid one whose i-face Mach numbers pass |M| > 1 (both split branches)
+    c = C.flat_plate_case(tmp, "fp_ausm", 41, 21, 0.3, 1e6, 1e-4, 1.08, lhs_order=1)
+    c.flux = "ausm"
+    C.write_inp(os.path.join(tmp, "fp_ausm.inp"), c)
+    yield "fp_ausm", c, 29
+    c = C.flat_plate_case(tmp, "ausm_sup", 33, 17, 1.5, 1e6, 1e-3, 1.1, lhs_order=1)
+    c.mu_inf = 0.0
+    c.flux = "ausm"
+    c.boundaries = [C.Boundary("slipwall", "bottom", 1, -2), C.Boundary("freestream", "top", 0, -1),
+                    C.Boundary("freestream", "left", 0, -1), C.Boundary("outflow", "right", 0, -1)]
+    C.write_inp(os.path.join(tmp, "ausm_sup.inp"), c)
+    yield "ausm_sup", c, 31
 
 
 def io_fixture(tmp: str):

@@ -73,11 +73,12 @@ def test_uniform_flow_preserved_on_device(gpu_lib, tmp_path):
     assert np.abs(r).max() < 1e-11
 
 
-@pytest.mark.parametrize("turb", ["none", "sa"])
-def test_jvp_matches_oracle(gpu_lib, port_built, tmp_path, turb):
+@pytest.mark.parametrize("turb,flux", [("none", "roe"), ("sa", "roe"), ("none", "ausm"), ("sa", "ausm")])
+def test_jvp_matches_oracle(gpu_lib, port_built, tmp_path, turb, flux):
     import torch
     from oracle.port import PortCase
     c = flat_plate(tmp_path, "jvp", 33, 21, turbulence=turb)
+    c.flux = flux
     xv, yv = C.load_grid(c)
     q = C.perturbed_state(c, 23)
     rng = np.random.default_rng(5)

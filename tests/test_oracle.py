@@ -36,11 +36,14 @@ def test_port_matches_reference_live(port_built, ref_available, tmp_path):
     assert rel_err(p.residual(q), ref.residual(q), p.flux_scale(q)) < 1e-13
 
 
-@pytest.mark.parametrize("turb", ["none", "sa", "sa_neg"])
+@pytest.mark.parametrize("turb", ["none", "sa", "sa_neg", "ausm"])
 def test_port_jvp_matches_central_fd(port_built, tmp_path, turb):
-    """sa_neg: a patch of negative nu_tilde (the SA-neg branches)."""
+    """sa_neg: a patch of negative nu_tilde (the SA-neg branches); ausm: the
+    AUSM flux (laminar)."""
     from oracle.port import PortCase
-    c = flat_plate(tmp_path, "jvp_" + turb, 25, 17, turbulence=turb[:2] if turb != "none" else turb)
+    c = flat_plate(tmp_path, "jvp_" + turb, 25, 17, turbulence={"sa": "sa", "sa_neg": "sa"}.get(turb, "none"))
+    if turb == "ausm":
+        c.flux = "ausm"
     p = PortCase(c)
     q = negative_nut_state(c, 5) if turb == "sa_neg" else C.perturbed_state(c, 5)
     rng = np.random.default_rng(1)
