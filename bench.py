@@ -174,6 +174,22 @@ def cpu_baseline_sample(turbulence: str, budget_s: float, threads: int, with_adj
                       % (n, what, turbulence, n * dt)}
 
 
+def max_over_ranks(x: float, world: int, device: str = "cuda") -> float:
+    """The slowest rank's figure (every rank gets it): replicas are timed
+    independently, and the job is as slow as its slowest replica."""
+    if world <= 1:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(world: int, cells: int, steps: int, seconds: float) -> float:
+    """Whole-job Mcells/s: every replica processes `cells` per step."""
+    return world * cells * steps / seconds / 1e6
+
+
 def run_reference(args, world, rank):
     if rank != 0:
         return
@@ -277,13 +293,9 @@ def run_ours(args, world, rank, local):
             step()
         ev1.record(stream)
         torch.cuda.synchronize()
-    el_ms = ev0.elapsed_time(ev1)
-    if world > 1:
-        t = torch.tensor([el_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        el_ms = float(t.item())
+    el_ms = max_over_ranks(ev0.elapsed_time(ev1), world, "cuda")
     ms_step = el_ms / args.steps
-    value = world * cells * args.steps / (el_ms * 1e-3) / 1e6
+    value = job_rate(world, cells, args.steps, el_ms * 1e-3)
 
     # per-launch attribution (outside the timed region)
     kern_res = eq.profile("residual")
@@ -320,15 +332,11 @@ def run_ours(args, world, rank, local):
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         e2e_step()
-    e2e_s = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([e2e_s], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world, "cuda")
     nq = c.nq
     h2d = cells * nq * 8 * (2 if with_adj else 1)
     d2h = cells * nq * 8 * (2 if with_adj else 1) + (cells * 8 if with_adj else 0)
-    e2e = {"value": world * cells * e2e_steps / e2e_s / 1e6, "unit": "Mcells/s",
+    e2e = {"value": job_rate(world, cells, e2e_steps, e2e_s), "unit": "Mcells/s",
            "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
 
     if rank != 0:
