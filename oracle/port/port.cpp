@@ -940,6 +940,35 @@ int port_vjp(void* hp, const double* q, const double* beta, const double* psi,
     const int nseeds = 25 * (nq + 1);
     if (out_q) std::memset(out_q, 0, n * 8);
     if (out_b) std::memset(out_b, 0, nc * 8);
+    // Wake and periodic boundaries couple cells far apart (bc.cpp:224-263,
+    // 329-364): a 5x5 colouring would alias their rows, so each cell is seeded
+    // alone and psi is dotted with every row (exact, dense; small grids).
+    bool nonlocal = false;
+    for (const auto& b : pc.bcs) nonlocal |= (b.type == ST_BC_WAKE || b.type == ST_BC_PERIODIC);
+    if (nonlocal) {
+#pragma omp parallel
+        {
+            std::vector<Dual> qd(n), bd(nc), rd(n);
+            Work<Dual> w;
+            w.init(pc);
+#pragma omp for schedule(dynamic, 8)
+            for (long s = 0; s < (long)(nc * (nq + 1)); s++) {
+                const size_t cell = (size_t)s / (nq + 1);
+                const int comp = (int)(s % (nq + 1));
+                if (comp == nq && (!out_b || !pc.sa)) continue;
+                for (size_t i = 0; i < n; i++) qd[i] = Dual(q[i], 0.0);
+                for (size_t i = 0; i < nc; i++) bd[i] = Dual(beta ? beta[i] : 1.0, 0.0);
+                if (comp < nq) qd[cell * nq + comp].d = 1.0;
+                else bd[cell].d = 1.0;
+                residual<Dual>(pc, qd.data(), bd.data(), rd.data(), order, w);
+                double acc = 0.0;
+                for (size_t r = 0; r < n; r++) acc += psi[r] * rd[r].d;
+                if (comp < nq) { if (out_q) out_q[cell * nq + comp] = acc; }
+                else out_b[cell] = acc;
+            }
+        }
+        return 0;
+    }
 #pragma omp parallel for schedule(dynamic, 1)
     for (int s = 0; s < nseeds; s++) {
         int colour = s / (nq + 1), comp = s % (nq + 1);

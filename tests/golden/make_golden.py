@@ -53,6 +53,15 @@ def cases(tmp: str):
                     C.Boundary("freestream", "left", 0, -1), C.Boundary("outflow", "right", 0, -1)]
     C.write_inp(os.path.join(tmp, "ausm_sup.inp"), c)
     yield "ausm_sup", c, 31
+    # the wake cut of the reference's NACA0012 C-grid example (bc.cpp:224-263): bottom
+    # cells 1..tail exchange ghosts with cells nic+1-i..; no-slip wall between
+    c = C.flat_plate_case(tmp, "wake", 41, 21, 0.5, 1e5, 1e-3, 1.1, lhs_order=1)
+    tail = 8
+    c.boundaries = [C.Boundary("freestream", "top", 0, -1), C.Boundary("freestream", "left", 0, -1),
+                    C.Boundary("freestream", "right", 0, -1), C.Boundary("wake", "bottom", 1, tail),
+                    C.Boundary("wall", "bottom", tail + 1, c.ni - 1 - tail)]
+    C.write_inp(os.path.join(tmp, "wake.inp"), c)
+    yield "wake", c, 37
 
 
 def io_fixture(tmp: str):

@@ -127,3 +127,18 @@ def test_grid_and_inp_roundtrip(tmp_path):
     assert c2.ni == c.ni and c2.mu_inf == c.mu_inf and len(c2.boundaries) == len(c.boundaries)
     assert [b.type for b in c2.boundaries] == [b.type for b in c.boundaries]
     assert c2.boundaries[0].face == "bottom" and c2.i_le == c.i_le
+
+
+@pytest.mark.parametrize("name", ["wake", "channel"])
+def test_port_vjp_transposes_jvp_with_nonlocal_boundaries(port_built, name):
+    """Wake and periodic boundaries couple distant cells; the oracle's
+    transposed product must still satisfy psi . (J v) = (J^T psi) . v."""
+    from oracle.port import PortCase
+    c, g = load_golden(name)
+    p = PortCase(c, g["xv"], g["yv"])
+    rng = np.random.default_rng(5)
+    v = rng.standard_normal(g["q"].shape)
+    psi = rng.standard_normal(g["q"].shape)
+    oq, _ = p.vjp(g["q"], psi)
+    lhs = float((psi * p.jvp(g["q"], v)).sum())
+    assert abs(lhs - float((oq * v).sum())) <= 1e-12 * abs(lhs)
