@@ -78,6 +78,27 @@ def cf_adjoint_gradient(eq: EulerEquation, w: np.ndarray, rtol: float = 1e-10, m
     return -ob.cpu().numpy(), st
 
 
+def lbfgs_direction(g: np.ndarray, S: list, Y: list, first_step: float = 1e-2) -> np.ndarray:
+    """-H g by the L-BFGS two-loop recursion over the pairs (s_k, y_k), oldest
+    first, with the initial scaling s.y / y.y of the newest pair; without
+    pairs, steepest descent scaled so that its largest entry is `first_step`."""
+    d = -g.copy()
+    alphas = []
+    for s, y in reversed(list(zip(S, Y))):
+        a = (s * d).sum() / (y * s).sum()
+        alphas.append(a)
+        d -= a * y
+    if S:
+        s, y = S[-1], Y[-1]
+        d *= (s * y).sum() / (y * y).sum()
+    else:
+        d *= first_step / max(np.abs(g).max(), 1e-300)
+    for (s, y), a in zip(zip(S, Y), reversed(alphas)):
+        b = (y * d).sum() / (y * s).sum()
+        d += (a - b) * s
+    return d
+
+
 @dataclasses.dataclass
 class InversionResult:
     beta: np.ndarray
@@ -132,21 +153,7 @@ def invert(eq: EulerEquation, xv: np.ndarray, cf_target: np.ndarray, q_start: np
     S, Y = [], []
     it = 0
     for it in range(1, max_iter + 1):
-        # two-loop recursion
-        d = -g.copy()
-        alphas = []
-        for s, y in reversed(list(zip(S, Y))):
-            a = (s * d).sum() / (y * s).sum()
-            alphas.append(a)
-            d -= a * y
-        if S:
-            s, y = S[-1], Y[-1]
-            d *= (s * y).sum() / (y * y).sum()
-        else:
-            d *= 1e-2 / max(np.abs(g).max(), 1e-300)
-        for (s, y), a in zip(zip(S, Y), reversed(alphas)):
-            b = (y * d).sum() / (y * s).sum()
-            d += (a - b) * s
+        d = lbfgs_direction(g, S, Y)
         gd = float((g * d).sum())
         if gd >= 0:
             d, gd = -g, -float((g * g).sum())

@@ -59,6 +59,10 @@ def gradient_check(ncells: int = 64, ni: int = 545, nj: int = 385, h: float = 1e
     eq.set_state(C.freestream_state(c))
     t0 = time.time()
     ok, hist = inv.converge(eq)
+    if hist is None:
+        out["flow_solve"] = {"converged": False, "diverged": True, "wall_s": time.time() - t0}
+        save("flow solve")
+        return out
     out["flow_solve"] = {"converged": bool(ok), "steps": int(hist.shape[0] - 1), "wall_s": time.time() - t0,
                          "residual_initial": float(hist[0, 3:].max()), "residual_final": float(hist[-1, 3:].max())}
     save("flow solve")
