@@ -1017,6 +1017,31 @@ int port_objective_grad(void* hp, const double* q, double* dJdq) {
         double x0 = pc.xv[(size_t)i * pc.nj], x1 = pc.xv[(size_t)(i + 1) * pc.nj];
         if (0.5 * (x0 + x1) <= pc.c.plate_x_end) dx[i] = x1 - x0;
     }
+    // a wake ghost reaches a distant column (see port_vjp): seed the first
+    // three rows cell by cell and sum over every face
+    bool nonlocal = false;
+    for (const auto& b : pc.bcs) nonlocal |= (b.type == ST_BC_WAKE || b.type == ST_BC_PERIODIC);
+    if (nonlocal) {
+        const int rows = std::min(3, njc);
+#pragma omp parallel
+        {
+            std::vector<Dual> qd(n), bd(nc), rd(n), cf(nic);
+            Work<Dual> w;
+            w.init(pc);
+#pragma omp for schedule(dynamic, 4)
+            for (long s = 0; s < (long)nic * rows * nq; s++) {
+                const int comp = (int)(s % nq), j = (int)((s / nq) % rows), i = (int)(s / nq / rows);
+                for (size_t t = 0; t < n; t++) qd[t] = Dual(q[t], 0.0);
+                for (size_t t = 0; t < nc; t++) bd[t] = Dual(1.0, 0.0);
+                qd[((size_t)i * njc + j) * nq + comp].d = 1.0;
+                residual<Dual>(pc, qd.data(), bd.data(), rd.data(), pc.c.order, w, cf.data());
+                double acc = 0.0;
+                for (int ii = 0; ii < nic; ii++) acc += dx[ii] * cf[ii].d;
+                dJdq[((size_t)i * njc + j) * nq + comp] = acc;
+            }
+        }
+        return 0;
+    }
 #pragma omp parallel for schedule(dynamic, 1)
     for (int s = 0; s < 25 * nq; s++) {
         int colour = s / nq, comp = s % nq, ci = colour / 5, cj = colour % 5;

@@ -142,3 +142,17 @@ def test_port_vjp_transposes_jvp_with_nonlocal_boundaries(port_built, name):
     oq, _ = p.vjp(g["q"], psi)
     lhs = float((psi * p.jvp(g["q"], v)).sum())
     assert abs(lhs - float((oq * v).sum())) <= 1e-12 * abs(lhs)
+
+
+def test_port_objective_gradient_with_wake_matches_fd(port_built):
+    """dJ/dQ where the plate's first faces read wake-cut ghosts (a distant
+    column) against central differences."""
+    from oracle.port import PortCase
+    c, g = load_golden("wake")
+    c.i_le = 9  # the no-slip wall's first vertex in this fixture
+    p = PortCase(c, g["xv"], g["yv"])
+    q = g["q"]
+    v = np.random.default_rng(2).standard_normal(q.shape) * np.abs(q).mean(axis=(0, 1))
+    h = 1e-6
+    fd = (p.skin_friction(q + h * v)[1] - p.skin_friction(q - h * v)[1]) / (2 * h)
+    assert abs(float((p.objective_grad(q) * v).sum()) - fd) <= 1e-8 * abs(fd)
