@@ -7,8 +7,9 @@
  * Conventions (all entry points):
  *   - return int status: ST_OK (0) or a negative ST_ERR_* code; the message
  *     of the last failure on the calling thread is st_last_error();
- *   - the caller owns host buffers, the context owns device buffers; there is
- *     no allocation per call after st_create (except where stated);
+ *   - the caller owns host buffers, the context owns device buffers; the
+ *     solver, adjoint, explicit-stage and MLP buffers are allocated on their
+ *     first use and kept; no other call allocates (except where stated);
  *   - one context = one device + one CUDA stream; calls on one context are
  *     not thread safe;
  *   - state layout is the reference's q[i][j][k]: cells i in [0,nic),
@@ -33,7 +34,7 @@ enum {
     ST_ERR_CUDA = -2,         /* CUDA runtime / launch failure */
     ST_ERR_NONFINITE = -3,    /* NaN/Inf detected in a result */
     ST_ERR_NOCONV = -4,       /* iterative solve did not converge */
-    ST_ERR_TIMEOUT = -5,      /* bounded device wait expired */
+    ST_ERR_TIMEOUT = -5,      /* bounded device wait expired (no current kernel waits on a flag) */
     ST_ERR_UNSUPPORTED = -6   /* option not built */
 };
 
@@ -147,7 +148,8 @@ int st_skin_friction(st_ctx* ctx, double* cf_host, double* J);
 /* Velocity gradients (u_x, u_y, v_x, v_y) of the current state at the j = 0
  * faces, [nic][4] on the host: the row of the reference's grad_u_eta /
  * grad_v_eta that IOManager::write_surface reads for Cf and the viscous
- * Cl/Cd (src/utils/io.cpp:217-236). */
+ * Cl/Cd (src/utils/io.cpp:217-236).  Uses a stream-ordered temporary of
+ * nic * 32 bytes. */
 int st_wall_gradients(st_ctx* ctx, double* out_host);
 
 /* Forward-mode Jacobian-vector product (dR/dQ) v + (dR/dbeta) vb on the
