@@ -360,7 +360,8 @@ int st_mlp_set_normalization(st_ctx* x, const float* mean, const float* stdev) {
 int st_mlp_enable(st_ctx* x, int on) {
     if (!x) return fail(ST_ERR_ARG, "st_mlp_enable: null context");
     if (on && !x->mlp_wb) return fail(ST_ERR_ARG, "st_mlp_enable: no network");
-    if (on && x->nq != 5) return fail(ST_ERR_UNSUPPORTED, "st_mlp_enable: needs the SA model");
+    if (on && (x->nq != 5 || !x->dc.viscous))  // features read the viscous face gradients
+        return fail(ST_ERR_UNSUPPORTED, "st_mlp_enable: needs the viscous SA model");
     x->dc.mlp_wb = on ? x->mlp_wb : nullptr;
     x->dc.mlp_wf = on ? x->mlp_wf : nullptr;
     return ST_OK;
