@@ -410,3 +410,76 @@ def channel_case(workdir: str, name: str, nj: int = 101, height: float = 0.1, ni
                          Boundary("periodic", "left", 0, -1)])
     write_inp(os.path.join(workdir, name + ".inp"), c)
     return c
+
+
+# --------------------------------------------------------------------------
+# C-grid around a NACA 0012 (the reference's examples/laminar/naca0012 setup)
+# --------------------------------------------------------------------------
+def naca0012_half_thickness(x: np.ndarray) -> np.ndarray:
+    """NACA four-digit thickness distribution for t = 0.12 with the closed
+    trailing edge variant (x^4 coefficient -0.1036)."""
+    return 0.6 * (0.2969 * np.sqrt(x) - 0.1260 * x - 0.3516 * x ** 2 + 0.2843 * x ** 3 - 0.1036 * x ** 4)
+
+
+def naca0012_cgrid(ni: int = 281, nj: int = 151, tail: int = 41, radius: float = 5.0, x_far: float = 6.0,
+                   h1: float = 1e-3, ratio: float = 1.1) -> Grid:
+    """C-grid by transfinite interpolation between the inner curve (lower wake
+    from x_far to the trailing edge, the section clockwise from the lower
+    trailing edge round the leading edge, upper wake back to x_far; vertices
+    0..tail-1 and ni-tail..ni-1 are the wake, which coincide pairwise) and an
+    outer C (a semicircle of `radius` about mid-chord joined to straight lines
+    out to x_far).  Inner and outer points correspond by the same parameter
+    per segment (x along the wakes, arc length round the section); j is
+    stretched from a first spacing of about h1."""
+    nbp = ni - 2 * tail + 1  # section panels (the reference's nb, mesh.cpp:349-350)
+    if nbp < 4 or nbp % 2:
+        raise ValueError("ni - 2 tail + 1 must be even and >= 4")
+    half = nbp // 2
+    theta = np.linspace(0.0, np.pi, half + 1)
+    xl = 0.5 * (1.0 + np.cos(theta))                      # 1 -> 0 (lower)
+    xs = np.concatenate([xl, xl[::-1][1:]])                # 1 -> 0 -> 1
+    ys = np.concatenate([-naca0012_half_thickness(xl), naca0012_half_thickness(xl[::-1][1:])])
+    ys[0] = ys[-1] = 0.0
+    dx_te = xs[0] - xs[1]
+    wake = 1.0 + stretched_spacing(tail - 1, dx_te, 1.05, x_far - 1.0)  # 1 -> x_far
+    xin = np.concatenate([wake[::-1], xs[1:-1], wake])
+    yin = np.concatenate([np.zeros(tail), ys[1:-1], np.zeros(tail)])
+    assert xin.size == ni
+    c0 = 0.5
+    xo = np.empty(ni)
+    yo = np.empty(ni)
+    wf = (wake - 1.0) / (x_far - 1.0)                      # 0 at the trailing edge
+    xo[:tail] = (c0 + wf * (x_far - c0))[::-1]
+    yo[:tail] = -radius
+    xo[ni - tail:] = c0 + wf * (x_far - c0)
+    yo[ni - tail:] = radius
+    seg = np.hypot(np.diff(xs), np.diff(ys))
+    f = np.concatenate([[0.0], np.cumsum(seg)]) / seg.sum()
+    phi = -0.5 * np.pi - np.pi * f
+    xo[tail - 1:ni - tail + 1] = c0 + radius * np.cos(phi)
+    yo[tail - 1:ni - tail + 1] = radius * np.sin(phi)
+    s = stretched_spacing(nj - 1, h1 / radius, ratio, 1.0)
+    xv = np.ascontiguousarray((1.0 - s)[None, :] * xin[:, None] + s[None, :] * xo[:, None])
+    yv = np.ascontiguousarray((1.0 - s)[None, :] * yin[:, None] + s[None, :] * yo[:, None])
+    return Grid(xv, yv, tail - 1)
+
+
+def naca0012_case(workdir: str, name: str, ni: int = 281, nj: int = 151, tail: int = 41, mach: float = 0.5,
+                  aoa_deg: float = 1.0, mu: float = 1e-4, write_files: bool = True, **grid) -> Case:
+    """The laminar NACA 0012 example's flow and boundaries (freestream on the
+    outer C and both outflow ends, wake cut on bottom cells 1..tail-1, no-slip
+    wall on the section) on the generated C-grid."""
+    g = naca0012_cgrid(ni, nj, tail, **grid)
+    grid_path = os.path.join(workdir, name + ".p3d")
+    a = math.radians(aoa_deg)
+    c = Case(grid_path=grid_path, ni=ni, nj=nj, u_inf=mach * math.cos(a), v_inf=mach * math.sin(a), mu_inf=mu,
+             pr_inf=0.7, aoa=aoa_deg, order=2, lhs_order=1, flux="roe", scheme="rk4_jameson", tail=tail,
+             label=os.path.join(workdir, name),
+             boundaries=[Boundary("freestream", "top", 0, -1), Boundary("freestream", "left", 0, -1),
+                         Boundary("freestream", "right", 0, -1), Boundary("wake", "bottom", 1, tail - 1),
+                         Boundary("wall", "bottom", tail, ni - tail)])
+    if write_files:
+        os.makedirs(workdir, exist_ok=True)
+        write_p3d(grid_path, g)
+        write_inp(os.path.join(workdir, name + ".inp"), c)
+    return c
