@@ -190,6 +190,19 @@ def job_rate(world: int, cells: int, steps: int, seconds: float) -> float:
     return world * cells * steps / seconds / 1e6
 
 
+def rate_breakdown(cells: int, res_ms: float, fused_ms: float | None) -> dict:
+    """Per-evaluation rates from the per-launch event times of one residual
+    pipeline and one fused residual+adjoint pipeline: residual alone, the
+    adjoint's share (fused minus residual) and the fused step."""
+    out = {"unit": "Mcells/s", "residual": cells / (res_ms * 1e-3) / 1e6, "residual_ms": res_ms}
+    if fused_ms:
+        out["fused_residual_adjoint"] = cells / (fused_ms * 1e-3) / 1e6
+        out["fused_ms"] = fused_ms
+        if fused_ms > res_ms:
+            out["adjoint_increment"] = cells / ((fused_ms - res_ms) * 1e-3) / 1e6
+    return out
+
+
 def run_reference(args, world, rank):
     if rank != 0:
         return
@@ -373,7 +386,8 @@ def run_ours(args, world, rank, local):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": workload_config(args, args.grid), "roofline": roof, "e2e": e2e,
-            "clocks": clk.summary(), "gpu_launches": kernels_per_step * args.steps}
+            "clocks": clk.summary(), "gpu_launches": kernels_per_step * args.steps,
+            "breakdown": rate_breakdown(cells, res_ms, adj_ms if with_adj else None)}
     if world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_sample(tb, 12.0, os.cpu_count() or 1, with_adj)
     print(json.dumps(line), flush=True)

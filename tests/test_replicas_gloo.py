@@ -41,3 +41,14 @@ def test_two_replicas_report_the_slowest_rank():
     slowest, rate = res[0]
     assert slowest == 2.0
     assert rate == pytest.approx(2 * 1_000_000 * 10 / 2.0 / 1e6)
+
+
+def test_rate_breakdown():
+    import importlib
+    sys.path.insert(0, ROOT)
+    bench = importlib.import_module("bench")
+    b = bench.rate_breakdown(8_000_000, 16.0, 40.0)
+    assert b["residual"] == pytest.approx(500.0)
+    assert b["fused_residual_adjoint"] == pytest.approx(200.0)
+    assert b["adjoint_increment"] == pytest.approx(8e6 / 24e-3 / 1e6)
+    assert "fused_residual_adjoint" not in bench.rate_breakdown(8_000_000, 16.0, None)
