@@ -29,3 +29,27 @@ def test_naca0012_thickness_is_twelve_percent():
     t = 2 * C.naca0012_half_thickness(x)
     assert abs(t.max() - 0.12) < 2e-4 and abs(x[t.argmax()] - 0.30) < 0.01
     assert abs(C.naca0012_half_thickness(np.array([1.0]))[0]) < 1e-12  # closed trailing edge
+
+
+def test_inp_round_trip_keeps_solver_and_boundary_keys(tmp_path):
+    c = C.naca0012_case(str(tmp_path), "rt", ni=41, nj=11, tail=11, write_files=False)
+    c.flux, c.scheme, c.cfl, c.cfl_ramp, c.iteration_max = "ausm", "forward_euler", 2.5, True, 77
+    c.grid_path = str(tmp_path / "rt.p3d")
+    C.write_p3d(c.grid_path, C.naca0012_cgrid(41, 11, 11))
+    path = str(tmp_path / "rt.inp")
+    C.write_inp(path, c)
+    r = C.read_inp(path)
+    for k in ("ni", "nj", "tail", "flux", "scheme", "cfl", "cfl_ramp", "iteration_max", "aoa", "u_inf", "v_inf",
+              "mu_inf", "order", "lhs_order"):
+        assert getattr(r, k) == getattr(c, k), k
+    assert [(b.type, b.face, b.start, b.end) for b in r.boundaries] == \
+        [(b.type, b.face, b.start, b.end) for b in c.boundaries]
+
+
+def test_missing_flux_key_reads_as_the_reference_default(tmp_path):
+    """config.cpp:54: solver.flux defaults to "ausm"."""
+    c = C.channel_case(str(tmp_path), "ch", nj=11)
+    path = str(tmp_path / "ch.inp")
+    text = open(path).read().replace('flux = "roe"\n', "")
+    open(path, "w").write(text)
+    assert C.read_inp(path).flux == "ausm"
