@@ -49,6 +49,7 @@ struct PCase {
     std::vector<st_bc> bcs;
     int ni, nj, nic, njc, nq;
     bool viscous, sa;
+    bool freeze_wake = false;  // wake ghosts copy values only (tangent 0)
     double R, cp;
     double eps_chi, eps_eta;
     std::vector<double> xv, yv, nchi, neta, vol, ds_chi, ds_eta, xc, yc, wd;
@@ -298,14 +299,18 @@ void apply_bcs(const PCase& pc, Work<T>& w) {
         case ST_BC_WAKE: {  // bc.cpp:224-263 (bottom/top only)
             if (!bottom_top) break;
             int je = (b.face == ST_FACE_BOTTOM) ? 0 : njc + 1;
-            for (int i = start; i <= end; i++) {
-                int g = w.P(i, je), s = w.P(nic + 1 - i, 1);
-                w.rho[g] = w.rho[s]; w.u[g] = w.u[s]; w.v[g] = w.v[s]; w.p[g] = w.p[s]; w.T_[g] = w.T_[s]; w.nut[g] = w.nut[s];
-            }
-            for (int i = start; i <= end; i++) {
-                int g = w.P(nic + 1 - i, je), s = w.P(i, 1);
-                w.rho[g] = w.rho[s]; w.u[g] = w.u[s]; w.v[g] = w.v[s]; w.p[g] = w.p[s]; w.T_[g] = w.T_[s]; w.nut[g] = w.nut[s];
-            }
+            // freeze_wake: the ghost takes the source's value with a zero
+            // tangent, so a JVP sees only the cells' local dependencies
+            auto cp = [&](int g, int s) {
+                if (pc.freeze_wake) {
+                    w.rho[g] = T(value(w.rho[s])); w.u[g] = T(value(w.u[s])); w.v[g] = T(value(w.v[s]));
+                    w.p[g] = T(value(w.p[s])); w.T_[g] = T(value(w.T_[s])); w.nut[g] = T(value(w.nut[s]));
+                } else {
+                    w.rho[g] = w.rho[s]; w.u[g] = w.u[s]; w.v[g] = w.v[s]; w.p[g] = w.p[s]; w.T_[g] = w.T_[s]; w.nut[g] = w.nut[s];
+                }
+            };
+            for (int i = start; i <= end; i++) cp(w.P(i, je), w.P(nic + 1 - i, 1));
+            for (int i = start; i <= end; i++) cp(w.P(nic + 1 - i, je), w.P(i, 1));
         } break;
         default: break;
         }
@@ -837,6 +842,13 @@ void* port_create(const st_case* c, const double* xv, const double* yv) {
 }
 
 void port_destroy(void* h) { delete static_cast<Handle*>(h); }
+
+// JVPs with the wake ghosts' tangents held at zero (the local part of the
+// Jacobian, as the implicit solver's colouring pass assembles it)
+int port_set_freeze_wake(void* hp, int on) {
+    static_cast<Handle*>(hp)->pc.freeze_wake = on != 0;
+    return 0;
+}
 
 int port_set_threads(int n) {
 #ifdef _OPENMP
