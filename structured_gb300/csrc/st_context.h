@@ -41,6 +41,12 @@ struct st_ctx {
     double* kzb = nullptr;   // flexible GMRES: preconditioned basis Z = M^{-1} V
     double* qtmp = nullptr;  // explicit RK stage state (Solution::q_tmp)
     float* lfac = nullptr;   // block ILU(0) factors, FP32: [cell][9][nq][nq]
+    // wake cut (bottom face): columns whose ghost copies a distant cell, and
+    // the partner blocks that coupling adds to the Jacobian: [nic][4][nq][nq]
+    std::vector<int> wake_cols;
+    int* wake_mask_d = nullptr;
+    double* wpart = nullptr;
+    bool wake_checked = false, has_wake = false;
     // learned SA correction: BF16 weights, FP32 biases + normalisation, FP32
     // master parameters with Adam moments, training partials
     void* mlp_wb = nullptr;
@@ -90,8 +96,10 @@ inline void mark(st_ctx* x, const char* name) {
 }
 // forward pipeline on (q -> rhs) for the double path; beta may be null
 int run_residual(st_ctx* ctx, const double* q, const double* beta, double* rhs, int order);
-// forward-mode JVP of the order-`order` residual at the context state (async)
-int run_jvp(st_ctx* ctx, const double* v_dev, const double* vb_dev, double* jv_dev, int order);
+// forward-mode JVP of the order-`order` residual at the context state (async);
+// freeze_wake holds the wake ghosts' tangents at zero (the Jacobian's local part)
+int run_jvp(st_ctx* ctx, const double* v_dev, const double* vb_dev, double* jv_dev, int order,
+            int freeze_wake = 0);
 // time step into ctx->dt (async)
 int run_dt(st_ctx* ctx, double cfl);
 // L2 norms of rhs into host out[nq] (synchronises)

@@ -45,6 +45,13 @@ __device__ inline void bc_copy(T* g, const T* s) {
     g[P_T] = s[P_T]; g[P_NUT] = s[P_NUT];
 }
 
+// value-only copy: a dual ghost keeps the source's value and a zero tangent
+template <class T>
+__device__ inline void bc_copy_value(T* g, const T* s) {
+    g[P_RHO] = T(val(s[P_RHO])); g[P_U] = T(val(s[P_U])); g[P_V] = T(val(s[P_V])); g[P_P] = T(val(s[P_P]));
+    g[P_T] = T(val(s[P_T])); g[P_NUT] = T(val(s[P_NUT]));
+}
+
 // All threads of the block apply c.bcs[0..nbc) in order.
 template <class T, int NQ>
 __device__ void bc_apply_block(const DevCase& c, T* __restrict__ P) {
@@ -134,12 +141,18 @@ __device__ void bc_apply_block(const DevCase& c, T* __restrict__ P) {
             }
         } else if (bc.type == 6) {  // wake, bc.cpp:224-263
             if (bt) {
+                // c.wake_frozen (the implicit solver's colouring JVPs): the
+                // cut's distant coupling is assembled separately
                 const int jg = (bc.face == 0) ? 0 : njc + 1;
-                for (int ip = start + threadIdx.x; ip <= end; ip += blockDim.x)
-                    bc_copy(P + pidx(c, ip, jg), P + pidx(c, nic + 1 - ip, 1));
+                for (int ip = start + threadIdx.x; ip <= end; ip += blockDim.x) {
+                    if (c.wake_frozen) bc_copy_value(P + pidx(c, ip, jg), P + pidx(c, nic + 1 - ip, 1));
+                    else bc_copy(P + pidx(c, ip, jg), P + pidx(c, nic + 1 - ip, 1));
+                }
                 __syncthreads();
-                for (int ip = start + threadIdx.x; ip <= end; ip += blockDim.x)
-                    bc_copy(P + pidx(c, nic + 1 - ip, jg), P + pidx(c, ip, 1));
+                for (int ip = start + threadIdx.x; ip <= end; ip += blockDim.x) {
+                    if (c.wake_frozen) bc_copy_value(P + pidx(c, nic + 1 - ip, jg), P + pidx(c, ip, 1));
+                    else bc_copy(P + pidx(c, nic + 1 - ip, jg), P + pidx(c, ip, 1));
+                }
             }
         }
         __syncthreads();

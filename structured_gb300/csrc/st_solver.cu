@@ -16,6 +16,7 @@
 
 #include "st_adjoint.cuh"
 #include "st_context.h"
+#include "st_wake.cuh"
 
 using namespace st;
 using stx::fail;
@@ -666,6 +667,55 @@ int ensure_solver(st_ctx* x, int m) {
     return ST_OK;
 }
 
+// Boundary list check for the implicit path and the wake column mask (once
+// per context).  Periodic boundaries and wake cuts other than a bottom cut
+// whose two halves lie WAKE_MIN_GAP or more columns apart are refused.
+int wake_setup(st_ctx* x) {
+    if (x->wake_checked) return ST_OK;
+    const int nic = x->c.ni - 1, njc = x->c.nj - 1;
+    std::vector<int> m(nic, 0);
+    int any = 0;
+    const char* why = "";
+    if (wake_columns(nic, njc, x->bcs.data(), (int)x->bcs.size(), m.data(), &any, &why))
+        return fail(ST_ERR_UNSUPPORTED, std::string("implicit solve: ") + why);
+    if (any) {
+        int rc = alloc_s(&x->wake_mask_d, (size_t)nic);
+        if (rc == ST_OK) rc = alloc_s(&x->wpart, (size_t)nic * NWS * x->nq * x->nq);
+        if (rc) return rc;
+        ST_CUDA(cudaMemcpyAsync(x->wake_mask_d, m.data(), nic * sizeof(int), cudaMemcpyHostToDevice, x->stream));
+        ST_CUDA(cudaStreamSynchronize(x->stream));
+    }
+    x->wake_cols = m;
+    x->has_wake = any != 0;
+    x->wake_checked = true;
+    return ST_OK;
+}
+
+// Wake partner blocks of the order-`order` residual into x->wpart
+// (2 halves x 3 residues x nq JVPs).
+int assemble_wake(st_ctx* x, int order) {
+    const int nq = x->nq, nic = x->c.ni - 1, njc = x->c.nj - 1;
+    cudaStream_t s = x->stream;
+    ST_CUDA(cudaMemsetAsync(x->wpart, 0, (size_t)nic * NWS * nq * nq * 8, s));
+    const unsigned g = grid_for(x->ncell), gw = grid_for((size_t)nic * NWS);
+    for (int side = 0; side < 2; side++)
+        for (int k = 0; k < 3; k++) {
+            bool seeded = false;
+            for (int i = 0; i < nic; i++) seeded |= x->wake_cols[i] && wake_side(i, nic) == side && i % 3 == k;
+            if (!seeded) continue;
+            for (int comp = 0; comp < nq; comp++) {
+                if (nq == 5) k_wake_seed<5><<<g, 256, 0, s>>>(nic, njc, x->wake_mask_d, side, k, comp, x->kz);
+                else k_wake_seed<4><<<g, 256, 0, s>>>(nic, njc, x->wake_mask_d, side, k, comp, x->kz);
+                int rc = stx::run_jvp(x, x->kz, nullptr, x->kw, order, 0);
+                if (rc) return rc;
+                if (nq == 5) k_wake_extract<5><<<gw, 256, 0, s>>>(nic, njc, x->wake_mask_d, side, k, comp, x->kw, x->wpart);
+                else k_wake_extract<4><<<gw, 256, 0, s>>>(nic, njc, x->wake_mask_d, side, k, comp, x->kw, x->wpart);
+            }
+        }
+    ST_LAUNCH_CHECK("wake partner assembly");
+    return ST_OK;
+}
+
 // Block Jacobian of the order-`order` residual at the context state into
 // `out` (x->jac or x->jac1).  A first-order Jacobian has the 9-point stencil,
 // so 9 colours suffice; second order needs 25.
@@ -680,7 +730,7 @@ int assemble_into(st_ctx* x, int order, double* out) {
             for (int comp = 0; comp < nq; comp++) {
                 if (nq == 5) k_seed<5><<<g, 256, 0, s>>>(nic, njc, cs, ci, cj, comp, x->kz);
                 else k_seed<4><<<g, 256, 0, s>>>(nic, njc, cs, ci, cj, comp, x->kz);
-                int rc = stx::run_jvp(x, x->kz, nullptr, x->kw, order);
+                int rc = stx::run_jvp(x, x->kz, nullptr, x->kw, order, x->has_wake ? 1 : 0);
                 if (rc) return rc;
                 if (nq == 5) k_extract<5><<<g, 256, 0, s>>>(nic, njc, cs, ci, cj, comp, x->kw, out);
                 else k_extract<4><<<g, 256, 0, s>>>(nic, njc, cs, ci, cj, comp, x->kw, out);
@@ -689,14 +739,19 @@ int assemble_into(st_ctx* x, int order, double* out) {
     return ST_OK;
 }
 
+// The operator's Jacobian: regular blocks and, with a wake cut, its partners.
 int assemble(st_ctx* x, int order) {
-    int rc = ensure_solver(x, 1);
-    if (rc) return rc;
-    return assemble_into(x, order, x->jac);
+    int rc = wake_setup(x);
+    if (rc == ST_OK) rc = ensure_solver(x, 1);
+    if (rc == ST_OK) rc = assemble_into(x, order, x->jac);
+    if (rc == ST_OK && x->has_wake) rc = assemble_wake(x, order);
+    return rc;
 }
 
 // Operator Jacobian (order `order`) and, for the preconditioner, the
-// first-order Jacobian (reusing the operator when it is first order).
+// first-order Jacobian (reusing the operator when it is first order).  The
+// preconditioner keeps the regular blocks only: the wake partners lie
+// outside the ILU(0) pattern.
 int assemble_pair(st_ctx* x, int order) {
     int rc = assemble(x, order);
     if (rc) return rc;
@@ -725,6 +780,16 @@ int apply_A(st_ctx* x, const LinOp& op, const double* in, double* out) {
     } else {
         if (op.trans) k_spmv<4, true><<<g, 256, 0, x->stream>>>(nic, njc, x->jac, in, out, op.dt, op.sd, op.sj);
         else k_spmv<4, false><<<g, 256, 0, x->stream>>>(nic, njc, x->jac, in, out, op.dt, op.sd, op.sj);
+    }
+    if (x->has_wake) {
+        const unsigned gw = grid_for((size_t)nic);
+        if (x->nq == 5) {
+            if (op.trans) k_wake_apply<5, true><<<gw, 256, 0, x->stream>>>(nic, njc, x->wpart, in, out, op.sj);
+            else k_wake_apply<5, false><<<gw, 256, 0, x->stream>>>(nic, njc, x->wpart, in, out, op.sj);
+        } else {
+            if (op.trans) k_wake_apply<4, true><<<gw, 256, 0, x->stream>>>(nic, njc, x->wpart, in, out, op.sj);
+            else k_wake_apply<4, false><<<gw, 256, 0, x->stream>>>(nic, njc, x->wpart, in, out, op.sj);
+        }
     }
     ST_LAUNCH_CHECK("spmv");
     return ST_OK;
@@ -883,9 +948,7 @@ extern "C" {
 
 int st_jacobian_assemble(st_ctx* x, int lhs) {
     if (!x) return fail(ST_ERR_ARG, "st_jacobian_assemble: null context");
-    for (const auto& b : x->bcs)
-        if (b.type == ST_BC_PERIODIC || b.type == ST_BC_WAKE)
-            return fail(ST_ERR_UNSUPPORTED, "st_jacobian_assemble: periodic/wake boundaries couple distant cells");
+    if (int rc0 = wake_setup(x)) return rc0;
     int rc = assemble_pair(x, lhs ? x->c.lhs_order : x->c.order);
     if (rc) return rc;
     ST_CUDA(cudaStreamSynchronize(x->stream));
@@ -928,9 +991,7 @@ int st_solve(st_ctx* x, const st_solve_params* p, st_solve_stats* stats, double*
              int* steps_done) {
     if (!x || !p) return fail(ST_ERR_ARG, "st_solve: null argument");
     if (p->max_steps < 0 || p->krylov_m < 1 || p->krylov_m > 500) return fail(ST_ERR_ARG, "st_solve: bad parameters");
-    for (const auto& b : x->bcs)
-        if (b.type == ST_BC_PERIODIC || b.type == ST_BC_WAKE)
-            return fail(ST_ERR_UNSUPPORTED, "st_solve: periodic/wake boundaries couple distant cells");
+    if (int rc0 = wake_setup(x)) return rc0;
     int rc = ensure_solver(x, p->krylov_m);
     if (rc) return rc;
     const int nq = x->nq;
@@ -1114,9 +1175,7 @@ int st_adjoint_solve_device(st_ctx* x, const double* b_dev, double* psi_dev, dou
                             double rtol, st_solve_stats* stats) {
     if (!x || !b_dev || !psi_dev) return fail(ST_ERR_ARG, "st_adjoint_solve_device: null argument");
     if (krylov_m < 1 || krylov_m > 500 || maxit < 1) return fail(ST_ERR_ARG, "st_adjoint_solve_device: krylov sizes");
-    for (const auto& b : x->bcs)
-        if (b.type == ST_BC_PERIODIC || b.type == ST_BC_WAKE)
-            return fail(ST_ERR_UNSUPPORTED, "st_adjoint_solve_device: periodic/wake boundaries couple distant cells");
+    if (int rc0 = wake_setup(x)) return rc0;
     // exact Jacobian of the residual actually solved (order, not lhs_order)
     int rc = assemble_pair(x, x->c.order);
     if (rc) return rc;
@@ -1134,9 +1193,7 @@ int st_tangent_solve_device(st_ctx* x, const double* b_dev, double* dq_dev, doub
                             double rtol, st_solve_stats* stats) {
     if (!x || !b_dev || !dq_dev) return fail(ST_ERR_ARG, "st_tangent_solve_device: null argument");
     if (krylov_m < 1 || krylov_m > 500 || maxit < 1) return fail(ST_ERR_ARG, "st_tangent_solve_device: krylov sizes");
-    for (const auto& b : x->bcs)
-        if (b.type == ST_BC_PERIODIC || b.type == ST_BC_WAKE)
-            return fail(ST_ERR_UNSUPPORTED, "st_tangent_solve_device: periodic/wake boundaries couple distant cells");
+    if (int rc0 = wake_setup(x)) return rc0;
     int rc = assemble_pair(x, x->c.order);
     if (rc) return rc;
     rc = stx::run_dt(x, cfl_prec);

@@ -1,0 +1,101 @@
+"""The implicit solver across the wake cut of a NACA 0012 C-grid on the GPU
+(bc.cpp:224-263 couples cell (a, 0) to the ghost below column nic-1-a):
+the assembled operator (regular blocks + wake partners) against the GPU's own
+JVP/VJP, its regular blocks against the oracle's frozen-wake colouring, and
+the pseudo-time Newton steady state against the oracle's (sparse LU Newton
+on the exact Jacobian, tests/block_jacobian.py) with Cl/Cd from the surface
+output."""
+import numpy as np
+import pytest
+
+import block_jacobian as BJ
+from structured_gb300 import case as C
+
+pytestmark = pytest.mark.gpu
+
+
+def naca(tmp_path, turbulence="none", ni=41, nj=9, tail=11):
+    c = C.naca0012_case(str(tmp_path), "naca", ni=ni, nj=nj, tail=tail)
+    c.turbulence = turbulence
+    return c, C.load_grid(c)
+
+
+def rel(a, b):
+    return float(np.abs(a - b).max() / (np.abs(b).max() + 1e-300))
+
+
+@pytest.mark.parametrize("turb", ["none", "sa"])
+@pytest.mark.parametrize("lhs", [False, True])
+def test_wake_operator_matches_jvp_and_vjp(gpu_lib, tmp_path, turb, lhs):
+    import torch
+    from structured_gb300.solver import EulerEquation
+    c, (xv, yv) = naca(tmp_path, turb)
+    q = C.perturbed_state(c, 41)
+    eq = EulerEquation(c, xv, yv)
+    eq.set_state(q)
+    eq.jacobian_assemble(lhs=lhs)
+    rng = np.random.default_rng(42)
+    v = torch.tensor(rng.standard_normal(q.shape) * np.abs(q).mean(axis=(0, 1)), device="cuda")
+    jv_ref = torch.empty_like(v)
+    eq.jvp_device(v.data_ptr(), jv_ref.data_ptr(), None, lhs=lhs)
+    jv = torch.empty_like(v)
+    eq.jacobian_apply_device(v.data_ptr(), jv.data_ptr())
+    torch.cuda.synchronize()
+    assert rel(jv.cpu().numpy(), jv_ref.cpu().numpy()) < 1e-12
+    psi = rng.standard_normal(q.shape)
+    oq, _ = eq.vjp(psi, lhs=lhs)
+    pt = torch.tensor(psi, device="cuda")
+    jt = torch.empty_like(pt)
+    eq.jacobian_apply_device(pt.data_ptr(), jt.data_ptr(), transpose=True)
+    torch.cuda.synchronize()
+    assert rel(jt.cpu().numpy(), oq) < 1e-11
+
+
+def test_wake_regular_blocks_match_oracle_colouring(gpu_lib, port_built, tmp_path):
+    from oracle.port import PortCase
+    from structured_gb300.solver import EulerEquation
+    c, (xv, yv) = naca(tmp_path, "sa")
+    q = C.perturbed_state(c, 43)
+    eq = EulerEquation(c, xv, yv)
+    eq.set_state(q)
+    eq.jacobian_assemble(lhs=False)
+    ours = eq.jacobian_blocks()
+    ref = BJ.assemble_regular(PortCase(c, xv, yv), q, 2)
+    # per row and component: relative to that row's largest entry
+    scale = np.abs(ref).max(axis=(2, 4), keepdims=True) + 1e-300
+    assert (np.abs(ours - ref) / scale).max() < 1e-10
+
+
+def test_wake_cut_newton_matches_oracle_steady_state(gpu_lib, port_built, tmp_path):
+    from oracle.port import PortCase
+    from structured_gb300 import io
+    from structured_gb300.solver import EulerEquation, Solver
+    c, (xv, yv) = naca(tmp_path, ni=61, nj=17, tail=13)
+    q0 = C.freestream_state(c)
+    eq = EulerEquation(c, xv, yv)
+    eq.set_state(q0)
+    ok, hist = Solver(eq, max_steps=200, cfl=1.0, cfl_ramp=0, cfl_growth=1.5, max_rel_drho=0.2, tolerance=1e-10,
+                      krylov_m=80, krylov_maxit=400, krylov_rtol=1e-6).solve()
+    assert ok, hist[-3:]
+    q_gpu = eq.get_state()
+    q_ref, h_ref = BJ.steady_newton(PortCase(c, xv, yv), c, q0)
+    assert h_ref[-1] < 1e-10
+    scale = np.abs(q_ref).max(axis=(0, 1))
+    assert (np.abs(q_gpu - q_ref).max(axis=(0, 1)) / scale).max() < 1e-8
+    f_gpu = io.write_outputs(eq, str(tmp_path / "gpu"))
+    eq.set_state(q_ref)
+    f_ref = io.write_outputs(eq, str(tmp_path / "ref"))
+    for k in ("cl", "cd", "cd_pressure", "cd_viscous"):
+        assert abs(f_gpu[k] - f_ref[k]) <= 1e-7 * (abs(f_ref["cd"]) + abs(f_ref["cl"])), k
+    assert f_ref["cd_viscous"] > 0 and f_ref["cd_pressure"] > 0
+
+
+def test_refused_boundary_lists(gpu_lib, tmp_path):
+    from structured_gb300.solver import EulerEquation, StructuredError
+    c, (xv, yv) = naca(tmp_path)
+    c.boundaries[3].end = 18          # the halves five columns apart
+    eq = EulerEquation(c, xv, yv)
+    eq.set_state(C.freestream_state(c))
+    with pytest.raises(StructuredError) as e:
+        eq.jacobian_assemble()
+    assert e.value.code == -6

@@ -110,3 +110,111 @@ def test_newton_on_the_wake_coupled_jacobian_converges_quadratically(port_built,
     # being purely quadratic); an inexact Jacobian settles at a fixed factor
     f = hist[-4:][1:] / hist[-4:][:-1]
     assert (np.diff(f) < 0).all() and f[-1] < 0.05, hist[-4:]
+
+
+GUARD = 64
+
+
+def guarded(n, fill=0.0, dtype=np.float64):
+    """Buffer of n elements inside NaN (or -7) guard bands; returns (whole, view)."""
+    g = np.full(n + 2 * GUARD, np.nan if dtype == np.float64 else -7, dtype=dtype)
+    g[GUARD:GUARD + n] = fill
+    return g, g[GUARD:GUARD + n]
+
+
+def guards_intact(g):
+    a, b = g[:GUARD], g[-GUARD:]
+    if g.dtype == np.float64:
+        return bool(np.isnan(a).all() and np.isnan(b).all())
+    return bool((a == -7).all() and (b == -7).all())
+
+
+@pytest.fixture(scope="module")
+def wake_host(tmp_path_factory):
+    """tests/wake_kernels_host.cpp: the device source of the wake pass built
+    for the host."""
+    import ctypes
+    import os
+    import subprocess
+    here = os.path.dirname(os.path.abspath(__file__))
+    so = str(tmp_path_factory.mktemp("wake_host") / "libwake_host.so")
+    subprocess.run(["g++", "-std=c++17", "-O1", "-Wall", "-Wno-unknown-pragmas", "-shared", "-fPIC", "-o", so,
+                    os.path.join(here, "wake_kernels_host.cpp")], check=True)
+    lib = ctypes.CDLL(so)
+    P = ctypes.c_void_p
+    I = ctypes.c_int
+    lib.wh_columns.argtypes = [I, I, P, I, P, P]
+    lib.wh_seed.argtypes = [I, I, I, P, I, I, I, P]
+    lib.wh_extract.argtypes = [I, I, I, P, I, I, I, P, P]
+    lib.wh_apply.argtypes = [I, I, I, I, P, P, P, ctypes.c_double]
+    return lib
+
+
+def host_columns(lib, c):
+    import ctypes
+    from structured_gb300 import abi
+    s, keep = abi.make_case_struct(c)
+    nic = c.ni - 1
+    gm, m = guarded(nic, 0, np.int32)
+    anyw = ctypes.c_int(-1)
+    rc = lib.wh_columns(nic, c.nj - 1, ctypes.cast(s.bcs, ctypes.c_void_p), s.nbc, m.ctypes.data,
+                        ctypes.byref(anyw))
+    assert guards_intact(gm)
+    return rc, m.astype(bool), anyw.value
+
+
+def test_host_build_of_wake_mask_agrees(wake_host, tmp_path):
+    c = C.naca0012_case(str(tmp_path), "n", ni=41, nj=9, tail=11, write_files=False)
+    rc, m, anyw = host_columns(wake_host, c)
+    assert rc == 0 and anyw == 1
+    assert np.array_equal(m, BJ.wake_columns(c))
+    c.boundaries[3].end = 18
+    assert host_columns(wake_host, c)[0] == -6
+    c.boundaries[3].end, c.boundaries[3].start = 10, 0
+    assert host_columns(wake_host, c)[0] == -6
+    c.boundaries[3].start, c.boundaries[3].face = 1, "top"
+    assert host_columns(wake_host, c)[0] == -6
+    c.boundaries[3].type = "freestream"
+    rc, m, anyw = host_columns(wake_host, c)
+    assert rc == 0 and anyw == 0 and not m.any()
+    ch = C.channel_case(str(tmp_path), "ch", nj=11)
+    assert host_columns(wake_host, ch)[0] == -6          # periodic
+
+
+@pytest.mark.parametrize("turbulence,order", [("none", 2), ("sa", 2), ("sa", 1)])
+def test_host_build_of_wake_pass_matches_restatement(port_built, wake_host, tmp_path, turbulence, order):
+    """The device source's seeds, extraction and products (run on the host over
+    the oracle's JVPs) equal the numpy layout, and touch nothing outside their
+    buffers."""
+    c, port = naca(tmp_path, turbulence)
+    q = C.perturbed_state(c, 13)
+    nic, njc, nq = q.shape
+    rc, m, _ = host_columns(wake_host, c)
+    assert rc == 0
+    mask = np.ascontiguousarray(m.astype(np.int32))
+    gW, W = guarded(nic * 4 * nq * nq)
+    for side in (0, 1):
+        for k in range(3):
+            for comp in range(nq):
+                gv, v = guarded(q.size, 5.0)
+                wake_host.wh_seed(nq, nic, njc, mask.ctypes.data, side, k, comp, v.ctypes.data)
+                assert guards_intact(gv)
+                jv = port.jvp(q, np.ascontiguousarray(v.reshape(q.shape)), lhs=(order == 1))
+                gj, jvb = guarded(q.size)
+                jvb[:] = jv.ravel()
+                wake_host.wh_extract(nq, nic, njc, mask.ctypes.data, side, k, comp, jvb.ctypes.data, W.ctypes.data)
+                assert guards_intact(gj) and guards_intact(gW)
+    ref = BJ.assemble_partners(port, q, BJ.wake_columns(c), order)
+    assert np.array_equal(W.reshape(ref.shape), ref)
+    zero = np.zeros((nic, njc, len(BJ.OFFSETS), nq, nq))
+    rng = np.random.default_rng(5)
+    for trans in (0, 1):
+        gx, x = guarded(q.size)
+        x[:] = rng.standard_normal(q.size)
+        gy, y = guarded(q.size)
+        y0 = rng.standard_normal(q.size)
+        y[:] = y0
+        wake_host.wh_apply(nq, trans, nic, njc, W.ctypes.data, x.ctypes.data, y.ctypes.data, -1.5)
+        assert guards_intact(gx) and guards_intact(gy) and guards_intact(gW)
+        want = y0 - 1.5 * BJ.apply(zero, ref, x.reshape(q.shape), trans=bool(trans)).ravel()
+        assert np.abs(y - want).max() < 1e-14 * np.abs(want).max()
