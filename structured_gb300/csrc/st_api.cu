@@ -556,7 +556,7 @@ int st_destroy(st_ctx* x) {
                       x->geo_i, x->geo_j, x->wd, x->nchi_d, x->neta_d, x->dsmin_d, x->dt, x->norm_part, x->norm_out,
                       x->cf, x->wall_dx_d, x->Pbar, x->srec, x->arec_i, x->arec_j, x->psi_tmp,
                       x->outq_tmp, x->outb_tmp, x->tape, x->jac, x->jac1, x->kv, x->kzb, x->kz, x->kw, x->kr, x->kh, x->kpart, x->dq, x->qsave,
-                      x->qtmp, x->wpart};
+                      x->qtmp, x->wpart, x->wallg};
     for (double* b : bufs) if (b) cudaFree(b);
     if (x->wake_mask_d) cudaFree(x->wake_mask_d);
     st::dual* dbufs[] = {x->qd, x->Pd, x->limd, x->Fdi, x->Fdj, x->Gdi, x->Gdj, x->rhsd, x->betad};
@@ -692,12 +692,13 @@ int st_wall_gradients(st_ctx* x, double* out_host) {
         k_bc<double, 4><<<1, 1024, 0, x->stream>>>(dc, x->P);
     }
     const int nic = x->c.ni - 1;
-    double* d = nullptr;
-    ST_CUDA(cudaMallocAsync((void**)&d, (size_t)nic * 4 * 8, x->stream));
-    k_wall_gradients<<<grid_for(nic), 256, 0, x->stream>>>(dc, x->P, d);
+    if (!x->wallg) {
+        int rc = alloc(&x->wallg, (size_t)nic * 4);
+        if (rc) return rc;
+    }
+    k_wall_gradients<<<grid_for(nic), 256, 0, x->stream>>>(dc, x->P, x->wallg);
     ST_LAUNCH_CHECK("wall gradients");
-    ST_CUDA(cudaMemcpyAsync(out_host, d, (size_t)nic * 4 * 8, cudaMemcpyDeviceToHost, x->stream));
-    ST_CUDA(cudaFreeAsync(d, x->stream));
+    ST_CUDA(cudaMemcpyAsync(out_host, x->wallg, (size_t)nic * 4 * 8, cudaMemcpyDeviceToHost, x->stream));
     ST_CUDA(cudaStreamSynchronize(x->stream));
     return ST_OK;
 }

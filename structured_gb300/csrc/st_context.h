@@ -40,6 +40,7 @@ struct st_ctx {
     double *kh = nullptr, *kpart = nullptr, *dq = nullptr, *qsave = nullptr;
     double* kzb = nullptr;   // flexible GMRES: preconditioned basis Z = M^{-1} V
     double* qtmp = nullptr;  // explicit RK stage state (Solution::q_tmp)
+    double* wallg = nullptr; // wall-face velocity gradients [nic][4] (st_wall_gradients)
     float* lfac = nullptr;   // block ILU(0) factors, FP32: [cell][9][nq][nq]
     // wake cut (bottom face): columns whose ghost copies a distant cell, and
     // the partner blocks that coupling adds to the Jacobian: [nic][4][nq][nq]
