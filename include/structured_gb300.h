@@ -148,8 +148,8 @@ int st_skin_friction(st_ctx* ctx, double* cf_host, double* J);
 /* Velocity gradients (u_x, u_y, v_x, v_y) of the current state at the j = 0
  * faces, [nic][4] on the host: the row of the reference's grad_u_eta /
  * grad_v_eta that IOManager::write_surface reads for Cf and the viscous
- * Cl/Cd (src/utils/io.cpp:217-236).  Uses a stream-ordered temporary of
- * nic * 32 bytes. */
+ * Cl/Cd (src/utils/io.cpp:217-236).  The first call allocates a context
+ * buffer of nic * 32 bytes. */
 int st_wall_gradients(st_ctx* ctx, double* out_host);
 
 /* Forward-mode Jacobian-vector product (dR/dQ) v + (dR/dbeta) vb on the
