@@ -178,18 +178,21 @@ int st_fused_launch_count(st_ctx* ctx, int lhs);
 /* Block Jacobian dR/dQ of the residual (lhs != 0: lhs_order) at the context
  * state, 13-point stencil of nq x nq blocks, from exact forward-mode JVPs over
  * a 5x5 cell colouring.  Replaces ADOL-C's sparse_jac and the COO buffers of
- * src/solver/solver.cpp:156-171.  A bottom wake cut (bc.cpp:224-263) adds,
- * per column, four blocks that couple rows (a-1,0), (a,0), (a+1,0), (a,1) to
- * cell (nic-1-a, 0); they are assembled too and used by every operator product
- * and solve below, but not by the preconditioner.  ST_ERR_UNSUPPORTED for
- * periodic BCs, a wake cut on another face or on a corner ghost, and a cut
- * whose two halves are less than 6 columns apart (this call, st_solve and the
- * adjoint and tangent solves). */
+ * src/solver/solver.cpp:156-171.  Ghosts that copy distant cells add blocks
+ * outside that stencil: a bottom wake cut (bc.cpp:224-263) and periodic
+ * boundaries in i (bc.cpp:329-365, the channel example).  Each copied ghost
+ * couples four rows next to its boundary to the cell it copies; those partner
+ * blocks are assembled too and used by every operator product and solve below,
+ * but not by the preconditioner.  ST_ERR_UNSUPPORTED (this call, st_solve and
+ * the adjoint and tangent solves) for a wake cut on another face or on a
+ * corner ghost, periodic boundaries in j or not covering every row, both kinds
+ * together, and grids one cell wide. */
 int st_jacobian_assemble(st_ctx* ctx, int lhs);
 /* Copy of the blocks, [nic][njc][13][nq][nq] (row component major); offsets
  * (di,dj): (0,0),(-1,0),(1,0),(0,-1),(0,1),(-2,0),(2,0),(0,-2),(0,2),
- * (-1,-1),(-1,1),(1,-1),(1,1).  With a wake cut these are the local part
- * (the wake ghosts held fixed); the cut's distant blocks are not copied. */
+ * (-1,-1),(-1,1),(1,-1),(1,1).  With wake or periodic boundaries these are
+ * the local part (the copied ghosts held fixed); the partner blocks are not
+ * copied. */
 int st_jacobian_blocks(st_ctx* ctx, double* blocks_host);
 /* out = J v (transpose != 0: J^T v) with the assembled blocks. */
 int st_jacobian_apply_device(st_ctx* ctx, const double* v_dev, double* out_dev, int transpose);

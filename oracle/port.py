@@ -41,7 +41,7 @@ def load():
         lib.port_jvp.argtypes = [ctypes.c_void_p, _P, _P, _P, _P, _P, ctypes.c_int]
         lib.port_vjp.argtypes = [ctypes.c_void_p, _P, _P, _P, _P, _P, ctypes.c_int]
         lib.port_objective_grad.argtypes = [ctypes.c_void_p, _P, _P]
-        lib.port_set_freeze_wake.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        lib.port_set_freeze_nonlocal.argtypes = [ctypes.c_void_p, ctypes.c_int]
         _lib = lib
     return _lib
 
@@ -124,10 +124,11 @@ class PortCase:
         self.lib.port_vjp(self.h, _ptr(q), _ptr(b), _ptr(psi), _ptr(oq), _ptr(ob), self._order(lhs))
         return oq, ob
 
-    def freeze_wake(self, on: bool = True) -> None:
-        """JVPs and VJPs with the wake ghosts' tangents held at zero: the
-        Jacobian's local part, without the wake cut's distant coupling."""
-        self.lib.port_set_freeze_wake(self.h, 1 if on else 0)
+    def freeze_nonlocal(self, on: bool = True) -> None:
+        """JVPs and VJPs with the periodic and wake ghosts' tangents held at
+        zero: the Jacobian's local part, without the distant coupling of those
+        boundary copies."""
+        self.lib.port_set_freeze_nonlocal(self.h, 1 if on else 0)
 
     def objective_grad(self, q):
         q = np.ascontiguousarray(q, dtype=np.float64)

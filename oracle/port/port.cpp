@@ -49,7 +49,7 @@ struct PCase {
     std::vector<st_bc> bcs;
     int ni, nj, nic, njc, nq;
     bool viscous, sa;
-    bool freeze_wake = false;  // wake ghosts copy values only (tangent 0)
+    bool freeze_nonlocal = false;  // periodic and wake ghosts copy values only (tangent 0)
     double R, cp;
     double eps_chi, eps_eta;
     std::vector<double> xv, yv, nchi, neta, vol, ds_chi, ds_eta, xc, yc, wd;
@@ -196,6 +196,19 @@ T laminar_mu(const PCase& pc, const T& temp) {
 // src/model/bc.cpp:430-433).  nut is SA's nu_tilde; its ghost rule per type is
 // this project's addition (wall: antisymmetric about 0, slip wall:
 // extrapolated like p and rho, freestream: nu_tilde_inf, others: copied).
+// Ghost g takes cell s's primitives (periodic and wake copies).  With
+// pc.freeze_nonlocal the copy carries the value only, so a JVP sees the
+// residual's local dependencies alone.
+template <class T>
+void copy_ghost(const PCase& pc, Work<T>& w, int g, int s) {
+    if (pc.freeze_nonlocal) {
+        w.rho[g] = T(value(w.rho[s])); w.u[g] = T(value(w.u[s])); w.v[g] = T(value(w.v[s]));
+        w.p[g] = T(value(w.p[s])); w.T_[g] = T(value(w.T_[s])); w.nut[g] = T(value(w.nut[s]));
+    } else {
+        w.rho[g] = w.rho[s]; w.u[g] = w.u[s]; w.v[g] = w.v[s]; w.p[g] = w.p[s]; w.T_[g] = w.T_[s]; w.nut[g] = w.nut[s];
+    }
+}
+
 template <class T>
 void apply_bcs(const PCase& pc, Work<T>& w) {
     const int nic = pc.nic, njc = pc.njc;
@@ -284,33 +297,21 @@ void apply_bcs(const PCase& pc, Work<T>& w) {
         case ST_BC_PERIODIC: {  // bc.cpp:329-365
             if (bottom_top) {
                 for (int i = start; i <= end; i++) {
-                    int g0 = w.P(i, 0), s0 = w.P(i, njc), g1 = w.P(i, njc + 1), s1 = w.P(i, 1);
-                    w.rho[g0] = w.rho[s0]; w.u[g0] = w.u[s0]; w.v[g0] = w.v[s0]; w.p[g0] = w.p[s0]; w.T_[g0] = w.T_[s0]; w.nut[g0] = w.nut[s0];
-                    w.rho[g1] = w.rho[s1]; w.u[g1] = w.u[s1]; w.v[g1] = w.v[s1]; w.p[g1] = w.p[s1]; w.T_[g1] = w.T_[s1]; w.nut[g1] = w.nut[s1];
+                    copy_ghost(pc, w, w.P(i, 0), w.P(i, njc));
+                    copy_ghost(pc, w, w.P(i, njc + 1), w.P(i, 1));
                 }
             } else {
                 for (int j = start; j <= end; j++) {
-                    int g0 = w.P(0, j), s0 = w.P(nic, j), g1 = w.P(nic + 1, j), s1 = w.P(1, j);
-                    w.rho[g0] = w.rho[s0]; w.u[g0] = w.u[s0]; w.v[g0] = w.v[s0]; w.p[g0] = w.p[s0]; w.T_[g0] = w.T_[s0]; w.nut[g0] = w.nut[s0];
-                    w.rho[g1] = w.rho[s1]; w.u[g1] = w.u[s1]; w.v[g1] = w.v[s1]; w.p[g1] = w.p[s1]; w.T_[g1] = w.T_[s1]; w.nut[g1] = w.nut[s1];
+                    copy_ghost(pc, w, w.P(0, j), w.P(nic, j));
+                    copy_ghost(pc, w, w.P(nic + 1, j), w.P(1, j));
                 }
             }
         } break;
         case ST_BC_WAKE: {  // bc.cpp:224-263 (bottom/top only)
             if (!bottom_top) break;
             int je = (b.face == ST_FACE_BOTTOM) ? 0 : njc + 1;
-            // freeze_wake: the ghost takes the source's value with a zero
-            // tangent, so a JVP sees only the cells' local dependencies
-            auto cp = [&](int g, int s) {
-                if (pc.freeze_wake) {
-                    w.rho[g] = T(value(w.rho[s])); w.u[g] = T(value(w.u[s])); w.v[g] = T(value(w.v[s]));
-                    w.p[g] = T(value(w.p[s])); w.T_[g] = T(value(w.T_[s])); w.nut[g] = T(value(w.nut[s]));
-                } else {
-                    w.rho[g] = w.rho[s]; w.u[g] = w.u[s]; w.v[g] = w.v[s]; w.p[g] = w.p[s]; w.T_[g] = w.T_[s]; w.nut[g] = w.nut[s];
-                }
-            };
-            for (int i = start; i <= end; i++) cp(w.P(i, je), w.P(nic + 1 - i, 1));
-            for (int i = start; i <= end; i++) cp(w.P(nic + 1 - i, je), w.P(i, 1));
+            for (int i = start; i <= end; i++) copy_ghost(pc, w, w.P(i, je), w.P(nic + 1 - i, 1));
+            for (int i = start; i <= end; i++) copy_ghost(pc, w, w.P(nic + 1 - i, je), w.P(i, 1));
         } break;
         default: break;
         }
@@ -843,10 +844,10 @@ void* port_create(const st_case* c, const double* xv, const double* yv) {
 
 void port_destroy(void* h) { delete static_cast<Handle*>(h); }
 
-// JVPs with the wake ghosts' tangents held at zero (the local part of the
-// Jacobian, as the implicit solver's colouring pass assembles it)
-int port_set_freeze_wake(void* hp, int on) {
-    static_cast<Handle*>(hp)->pc.freeze_wake = on != 0;
+// JVPs with the periodic and wake ghosts' tangents held at zero (the local
+// part of the Jacobian, as the implicit solver's colouring pass assembles it)
+int port_set_freeze_nonlocal(void* hp, int on) {
+    static_cast<Handle*>(hp)->pc.freeze_nonlocal = on != 0;
     return 0;
 }
 

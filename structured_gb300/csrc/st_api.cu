@@ -340,7 +340,7 @@ int order_of(st_ctx* x, int lhs) { return lhs ? x->c.lhs_order : x->c.order; }
 }  // namespace
 
 namespace stx {
-int run_jvp(st_ctx* x, const double* v_dev, const double* vb_dev, double* jv_dev, int order, int freeze_wake) {
+int run_jvp(st_ctx* x, const double* v_dev, const double* vb_dev, double* jv_dev, int order, int freeze_nonlocal) {
     const int nq = x->nq;
     if (!x->qd) {
         int rc = ST_OK;
@@ -362,7 +362,7 @@ int run_jvp(st_ctx* x, const double* v_dev, const double* vb_dev, double* jv_dev
     k_to_dual<<<grid_for(x->ncell * nq), 256, 0, s>>>(x->q, v_dev, x->qd, x->ncell * nq, 0.0);
     k_to_dual<<<grid_for(x->ncell), 256, 0, s>>>(x->beta, vb_dev, x->betad, x->ncell, 1.0);
     st::DevCase dc = x->dc;
-    dc.wake_frozen = freeze_wake;
+    dc.nonlocal_frozen = freeze_nonlocal;
     int rc;
     if (nq == 5)
         rc = launch_forward<st::dual, 5>(x, dc, x->qd, x->betad, x->Pd, x->limd, x->Fdi, x->Fdj,
@@ -542,7 +542,7 @@ int st_create(const st_case* c, const double* xv, const double* yv, int device, 
     dc.dpdx = c->dpdx; dc.dpdy = c->dpdy;
     dc.vol = x->vol_d; dc.ivol = x->ivol_d; dc.geo_i = x->geo_i; dc.geo_j = x->geo_j; dc.wd = x->wd;
     dc.nchi = x->nchi_d; dc.neta = x->neta_d; dc.bcs = x->bcs_d; dc.err = x->err_d;
-    dc.mlp_wb = nullptr; dc.mlp_wf = nullptr; dc.wake_frozen = 0;
+    dc.mlp_wb = nullptr; dc.mlp_wf = nullptr; dc.nonlocal_frozen = 0;
     cudaError_t e = cudaStreamSynchronize(x->stream);
     if (e != cudaSuccess) { st_destroy(x); return stx::cuda_fail(e, "st_create"); }
     *out = x;
@@ -556,9 +556,9 @@ int st_destroy(st_ctx* x) {
                       x->geo_i, x->geo_j, x->wd, x->nchi_d, x->neta_d, x->dsmin_d, x->dt, x->norm_part, x->norm_out,
                       x->cf, x->wall_dx_d, x->Pbar, x->srec, x->arec_i, x->arec_j, x->psi_tmp,
                       x->outq_tmp, x->outb_tmp, x->tape, x->jac, x->jac1, x->kv, x->kzb, x->kz, x->kw, x->kr, x->kh, x->kpart, x->dq, x->qsave,
-                      x->qtmp, x->wpart, x->wallg};
+                      x->qtmp, x->wpart[0], x->wpart[1], x->wpart[2], x->wallg};
     for (double* b : bufs) if (b) cudaFree(b);
-    if (x->wake_mask_d) cudaFree(x->wake_mask_d);
+    for (int* m : x->pmask_d) if (m) cudaFree(m);
     st::dual* dbufs[] = {x->qd, x->Pd, x->limd, x->Fdi, x->Fdj, x->Gdi, x->Gdj, x->rhsd, x->betad};
     for (st::dual* b : dbufs) if (b) cudaFree(b);
     if (x->bcs_d) cudaFree(x->bcs_d);

@@ -66,7 +66,7 @@ struct DevCase {
     int* err;              // device error flag
     const void* mlp_wb;    // learned beta: BF16 weight block (null: beta from the beta array)
     const float* mlp_wf;   // its FP32 biases and feature normalisation
-    int wake_frozen;       // wake ghosts take their source's value with a zero tangent
+    int nonlocal_frozen;   // periodic and wake ghosts take their source's value with a zero tangent
 };
 
 __host__ __device__ inline size_t pidx(const DevCase& c, int ip, int jp) {

@@ -42,12 +42,14 @@ struct st_ctx {
     double* qtmp = nullptr;  // explicit RK stage state (Solution::q_tmp)
     double* wallg = nullptr; // wall-face velocity gradients [nic][4] (st_wall_gradients)
     float* lfac = nullptr;   // block ILU(0) factors, FP32: [cell][9][nq][nq]
-    // wake cut (bottom face): columns whose ghost copies a distant cell, and
-    // the partner blocks that coupling adds to the Jacobian: [nic][4][nq][nq]
-    std::vector<int> wake_cols;
-    int* wake_mask_d = nullptr;
-    double* wpart = nullptr;
-    bool wake_checked = false, has_wake = false;
+    // non-local boundary copies (wake cut, periodic in i), per family: which
+    // ghosts are copies, and the partner blocks that coupling adds to the
+    // Jacobian, [line length][4][nq][nq] (st_partner.cuh)
+    std::vector<int> pmask[3];
+    int* pmask_d[3] = {nullptr, nullptr, nullptr};
+    double* wpart[3] = {nullptr, nullptr, nullptr};
+    bool partners_checked = false, has_partners = false;
+    bool pfam_on[3] = {false, false, false};
     // learned SA correction: BF16 weights, FP32 biases + normalisation, FP32
     // master parameters with Adam moments, training partials
     void* mlp_wb = nullptr;
@@ -98,9 +100,10 @@ inline void mark(st_ctx* x, const char* name) {
 // forward pipeline on (q -> rhs) for the double path; beta may be null
 int run_residual(st_ctx* ctx, const double* q, const double* beta, double* rhs, int order);
 // forward-mode JVP of the order-`order` residual at the context state (async);
-// freeze_wake holds the wake ghosts' tangents at zero (the Jacobian's local part)
+// freeze_nonlocal holds the periodic and wake ghosts' tangents at zero (the
+// Jacobian's local part)
 int run_jvp(st_ctx* ctx, const double* v_dev, const double* vb_dev, double* jv_dev, int order,
-            int freeze_wake = 0);
+            int freeze_nonlocal = 0);
 // time step into ctx->dt (async)
 int run_dt(st_ctx* ctx, double cfl);
 // L2 norms of rhs into host out[nq] (synchronises)

@@ -45,11 +45,17 @@ __device__ inline void bc_copy(T* g, const T* s) {
     g[P_T] = s[P_T]; g[P_NUT] = s[P_NUT];
 }
 
-// value-only copy: a dual ghost keeps the source's value and a zero tangent
+// Non-local copy (periodic, wake).  With c.nonlocal_frozen (the implicit
+// solver's colouring JVPs) a dual ghost keeps the source's value and a zero
+// tangent: the copies' distant coupling is assembled separately.
 template <class T>
-__device__ inline void bc_copy_value(T* g, const T* s) {
-    g[P_RHO] = T(val(s[P_RHO])); g[P_U] = T(val(s[P_U])); g[P_V] = T(val(s[P_V])); g[P_P] = T(val(s[P_P]));
-    g[P_T] = T(val(s[P_T])); g[P_NUT] = T(val(s[P_NUT]));
+__device__ inline void bc_copy_nl(const DevCase& c, T* g, const T* s) {
+    if (c.nonlocal_frozen) {
+        g[P_RHO] = T(val(s[P_RHO])); g[P_U] = T(val(s[P_U])); g[P_V] = T(val(s[P_V])); g[P_P] = T(val(s[P_P]));
+        g[P_T] = T(val(s[P_T])); g[P_NUT] = T(val(s[P_NUT]));
+    } else {
+        bc_copy(g, s);
+    }
 }
 
 // All threads of the block apply c.bcs[0..nbc) in order.
@@ -132,27 +138,21 @@ __device__ void bc_apply_block(const DevCase& c, T* __restrict__ P) {
         } else if (bc.type == 4) {  // periodic, bc.cpp:329-365
             for (int s = start + threadIdx.x; s <= end; s += blockDim.x) {
                 if (bt) {
-                    bc_copy(P + pidx(c, s, 0), P + pidx(c, s, njc));
-                    bc_copy(P + pidx(c, s, njc + 1), P + pidx(c, s, 1));
+                    bc_copy_nl(c, P + pidx(c, s, 0), P + pidx(c, s, njc));
+                    bc_copy_nl(c, P + pidx(c, s, njc + 1), P + pidx(c, s, 1));
                 } else {
-                    bc_copy(P + pidx(c, 0, s), P + pidx(c, nic, s));
-                    bc_copy(P + pidx(c, nic + 1, s), P + pidx(c, 1, s));
+                    bc_copy_nl(c, P + pidx(c, 0, s), P + pidx(c, nic, s));
+                    bc_copy_nl(c, P + pidx(c, nic + 1, s), P + pidx(c, 1, s));
                 }
             }
         } else if (bc.type == 6) {  // wake, bc.cpp:224-263
             if (bt) {
-                // c.wake_frozen (the implicit solver's colouring JVPs): the
-                // cut's distant coupling is assembled separately
                 const int jg = (bc.face == 0) ? 0 : njc + 1;
-                for (int ip = start + threadIdx.x; ip <= end; ip += blockDim.x) {
-                    if (c.wake_frozen) bc_copy_value(P + pidx(c, ip, jg), P + pidx(c, nic + 1 - ip, 1));
-                    else bc_copy(P + pidx(c, ip, jg), P + pidx(c, nic + 1 - ip, 1));
-                }
+                for (int ip = start + threadIdx.x; ip <= end; ip += blockDim.x)
+                    bc_copy_nl(c, P + pidx(c, ip, jg), P + pidx(c, nic + 1 - ip, 1));
                 __syncthreads();
-                for (int ip = start + threadIdx.x; ip <= end; ip += blockDim.x) {
-                    if (c.wake_frozen) bc_copy_value(P + pidx(c, nic + 1 - ip, jg), P + pidx(c, ip, 1));
-                    else bc_copy(P + pidx(c, nic + 1 - ip, jg), P + pidx(c, ip, 1));
-                }
+                for (int ip = start + threadIdx.x; ip <= end; ip += blockDim.x)
+                    bc_copy_nl(c, P + pidx(c, nic + 1 - ip, jg), P + pidx(c, ip, 1));
             }
         }
         __syncthreads();

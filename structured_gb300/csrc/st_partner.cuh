@@ -1,0 +1,175 @@
+// Partner blocks of the implicit solver's Jacobian: the coupling that the
+// non-local boundary copies add to the 13-point stencil (st_solver.cu
+// launches these kernels).
+//
+// Self-contained apart from the C header's boundary types, so that the same
+// source also compiles as plain C++ on a host (the qualifiers and the thread
+// indices then come from the includer) for CPU checks of its index arithmetic.
+#pragma once
+#include <cstddef>
+
+#include "../../include/structured_gb300.h"
+
+namespace st {
+
+// ---------------------------------------------------------------------------
+// Three families of ghosts are copies of cells elsewhere in the grid:
+//   FAM_WAKE   wake cut (bc.cpp:224-263): the bottom ghost below column b is a
+//              copy of cell (nic-1-b, 0);
+//   FAM_LEFT   periodic in i (bc.cpp:329-365): the ghost left of row b is a
+//              copy of cell (nic-1, b);
+//   FAM_RIGHT  the ghost right of row b is a copy of cell (0, b).
+// Ghost b of a family enters four residual rows: at distance 0 from its
+// boundary the rows at line positions b-1, b, b+1, at distance 1 the row at b
+// (wake: rows (b-1,0), (b,0), (b+1,0), (b,1); left: (0,b-1), (0,b), (0,b+1),
+// (1,b)).  A corner ghost that copies a wall ghost of the far column reaches
+// only rows already in these windows.  Partner slot t of line position p holds
+//   W_f[p][t] = d R(row f(p, t)) / d q(source of ghost p - wslot_d(t)),
+// the part of that block carried by the copy.  The regular 13-point blocks
+// come from a colouring pass whose JVPs hold every copy's tangent at zero; a
+// partner pass seeds the sources of the ghosts b = k mod 3 of one family (their
+// windows, three positions wide, share no row) and reads the difference of a
+// full and a frozen JVP, which is exactly the part carried by the copies.
+// ---------------------------------------------------------------------------
+constexpr int NWS = 4;
+enum { FAM_WAKE = 0, FAM_LEFT = 1, FAM_RIGHT = 2, NFAM = 3 };
+
+__host__ __device__ inline int wslot_j(int t) { return t == 3 ? 1 : 0; }     // distance from the boundary
+__host__ __device__ inline int wslot_d(int t) { return t == 3 ? 0 : t - 1; }  // row position - ghost position
+__host__ __device__ inline int fam_len(int f, int nic, int njc) { return f == FAM_WAKE ? nic : njc; }
+
+// cell index i * njc + j of the row of slot t at line position p
+__host__ __device__ inline size_t fam_row(int f, int p, int t, int nic, int njc) {
+    const int l = wslot_j(t);
+    const int i = f == FAM_WAKE ? p : (f == FAM_LEFT ? l : nic - 1 - l);
+    const int j = f == FAM_WAKE ? l : p;
+    return (size_t)i * njc + j;
+}
+
+// cell index of the cell that ghost b of family f copies
+__host__ __device__ inline size_t fam_src(int f, int b, int nic, int njc) {
+    if (f == FAM_WAKE) return (size_t)(nic - 1 - b) * njc;
+    if (f == FAM_LEFT) return (size_t)(nic - 1) * njc + b;
+    return (size_t)b;
+}
+
+// Ghost masks of the boundary list, in order: mask[f][b] = 1 if ghost b of
+// family f is a copy (mask[FAM_WAKE] has nic entries, the others njc);
+// on[f] = 1 if the family occurs.  Returns 0, or ST_ERR_UNSUPPORTED with *why
+// set for lists this layout cannot hold: a wake cut off the bottom face or on
+// a corner ghost, periodic boundaries on the bottom/top faces or not covering
+// every row, a wake cut together with periodic boundaries, fewer than two
+// cells across the grid.
+inline int partner_masks(int nic, int njc, const st_bc* bcs, int nbc, int* mask_wake, int* mask_left,
+                         int* mask_right, int* on, const char** why) {
+    for (int f = 0; f < NFAM; f++) on[f] = 0;
+    for (int i = 0; i < nic; i++) mask_wake[i] = 0;
+    for (int j = 0; j < njc; j++) mask_left[j] = mask_right[j] = 0;
+    for (int n = 0; n < nbc; n++) {
+        const st_bc& b = bcs[n];
+        if (b.type != ST_BC_WAKE && b.type != ST_BC_PERIODIC) continue;
+        const bool bt = b.face == ST_FACE_BOTTOM || b.face == ST_FACE_TOP;
+        const int end = b.end >= 0 ? b.end : (bt ? nic : njc) + 2 + b.end;
+        if (b.start > end) continue;
+        if (b.type == ST_BC_WAKE) {
+            if (b.face != ST_FACE_BOTTOM) { *why = "wake cut off the bottom face"; return ST_ERR_UNSUPPORTED; }
+            if (b.start < 1 || end > nic) { *why = "wake range on a corner ghost"; return ST_ERR_UNSUPPORTED; }
+            for (int ip = b.start; ip <= end; ip++) {
+                mask_wake[ip - 1] = 1;
+                mask_wake[nic - ip] = 1;
+            }
+            on[FAM_WAKE] = 1;
+        } else {
+            if (bt) { *why = "periodic boundaries on the bottom/top faces"; return ST_ERR_UNSUPPORTED; }
+            if (b.start > 1 || end < njc) { *why = "periodic range not covering every row"; return ST_ERR_UNSUPPORTED; }
+            for (int j = 0; j < njc; j++) mask_left[j] = mask_right[j] = 1;
+            on[FAM_LEFT] = on[FAM_RIGHT] = 1;
+        }
+    }
+    if (on[FAM_WAKE] && on[FAM_LEFT]) { *why = "a wake cut together with periodic boundaries"; return ST_ERR_UNSUPPORTED; }
+    if ((on[FAM_WAKE] || on[FAM_LEFT]) && (nic < 2 || njc < 2)) { *why = "fewer than two cells across"; return ST_ERR_UNSUPPORTED; }
+    return 0;
+}
+
+// v = 0 except unit `comp` at the sources of the family's ghosts b = k mod 3
+// (v zeroed beforehand); one thread per ghost
+template <int NQ>
+__global__ void k_partner_seed(int f, int nic, int njc, const int* __restrict__ mask, int k, int comp,
+                               double* __restrict__ v) {
+    const int n = fam_len(f, nic, njc);
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < n; b += gridDim.x * blockDim.x)
+        if (mask[b] && b % 3 == k) v[fam_src(f, b, nic, njc) * NQ + comp] = 1.0;
+}
+
+// W column `comp` of the slots whose ghost was seeded: full - frozen JVP
+template <int NQ>
+__global__ void k_partner_extract(int f, int nic, int njc, const int* __restrict__ mask, int k, int comp,
+                                  const double* __restrict__ jv_full, const double* __restrict__ jv_frozen,
+                                  double* __restrict__ W) {
+    const int len = fam_len(f, nic, njc), n = len * NWS;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const int p = t / NWS, slot = t % NWS;
+        const int b = p - wslot_d(slot);
+        if (b < 0 || b >= len || !mask[b] || b % 3 != k) continue;
+        const size_t row = fam_row(f, p, slot, nic, njc);
+        double* w = W + (size_t)t * NQ * NQ;
+#pragma unroll
+        for (int kk = 0; kk < NQ; kk++) w[kk * NQ + comp] = jv_full[row * NQ + kk] - jv_frozen[row * NQ + kk];
+    }
+}
+
+// acc += b x (TRANS: b^T x) for one nq x nq block
+template <int NQ, bool TRANS>
+__device__ inline void block_mv(const double* __restrict__ b, const double* __restrict__ x, double* acc) {
+#pragma unroll
+    for (int kk = 0; kk < NQ; kk++)
+#pragma unroll
+        for (int l = 0; l < NQ; l++) acc[kk] += (TRANS ? b[l * NQ + kk] : b[kk * NQ + l]) * x[l];
+}
+
+// y += sj * W x (or W^T x) for one family, after k_spmv on the same stream.
+// Forward: one thread per line position writes its two rows; transposed: one
+// thread per ghost gathers into the ghost's source cell (sources are
+// distinct), so neither needs atomics.
+template <int NQ, bool TRANS>
+__global__ void k_partner_apply(int f, int nic, int njc, const double* __restrict__ W,
+                                const double* __restrict__ x, double* __restrict__ y, double sj) {
+    const int len = fam_len(f, nic, njc);
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < len; p += gridDim.x * blockDim.x) {
+        if (!TRANS) {
+            double a0[NQ], a1[NQ];
+#pragma unroll
+            for (int kk = 0; kk < NQ; kk++) { a0[kk] = 0.0; a1[kk] = 0.0; }
+#pragma unroll
+            for (int slot = 0; slot < NWS; slot++) {
+                const int b = p - wslot_d(slot);
+                if (b < 0 || b >= len) continue;
+                const double* w = W + ((size_t)p * NWS + slot) * NQ * NQ;
+                const double* xs = x + fam_src(f, b, nic, njc) * NQ;
+                if (wslot_j(slot)) block_mv<NQ, false>(w, xs, a1);
+                else block_mv<NQ, false>(w, xs, a0);
+            }
+            double* y0 = y + fam_row(f, p, 0, nic, njc) * NQ;
+            double* y1 = y + fam_row(f, p, 3, nic, njc) * NQ;
+#pragma unroll
+            for (int kk = 0; kk < NQ; kk++) { y0[kk] += sj * a0[kk]; y1[kk] += sj * a1[kk]; }
+        } else {
+            const int b = p;  // this thread's ghost
+            double acc[NQ];
+#pragma unroll
+            for (int kk = 0; kk < NQ; kk++) acc[kk] = 0.0;
+#pragma unroll
+            for (int slot = 0; slot < NWS; slot++) {
+                const int r = b + wslot_d(slot);
+                if (r < 0 || r >= len) continue;
+                block_mv<NQ, true>(W + ((size_t)r * NWS + slot) * NQ * NQ, x + fam_row(f, r, slot, nic, njc) * NQ,
+                                   acc);
+            }
+            double* ys = y + fam_src(f, b, nic, njc) * NQ;
+#pragma unroll
+            for (int kk = 0; kk < NQ; kk++) ys[kk] += sj * acc[kk];
+        }
+    }
+}
+
+}  // namespace st

@@ -16,7 +16,7 @@
 
 #include "st_adjoint.cuh"
 #include "st_context.h"
-#include "st_wake.cuh"
+#include "st_partner.cuh"
 
 using namespace st;
 using stx::fail;
@@ -667,52 +667,62 @@ int ensure_solver(st_ctx* x, int m) {
     return ST_OK;
 }
 
-// Boundary list check for the implicit path and the wake column mask (once
-// per context).  Periodic boundaries and wake cuts other than a bottom cut
-// whose two halves lie WAKE_MIN_GAP or more columns apart are refused.
-int wake_setup(st_ctx* x) {
-    if (x->wake_checked) return ST_OK;
+// Boundary list check for the implicit path and the ghost masks of its
+// non-local copies (once per context).
+int partner_setup(st_ctx* x) {
+    if (x->partners_checked) return ST_OK;
     const int nic = x->c.ni - 1, njc = x->c.nj - 1;
-    std::vector<int> m(nic, 0);
-    int any = 0;
+    std::vector<int> m[NFAM] = {std::vector<int>(nic), std::vector<int>(njc), std::vector<int>(njc)};
+    int on[NFAM];
     const char* why = "";
-    if (wake_columns(nic, njc, x->bcs.data(), (int)x->bcs.size(), m.data(), &any, &why))
+    if (partner_masks(nic, njc, x->bcs.data(), (int)x->bcs.size(), m[0].data(), m[1].data(), m[2].data(), on, &why))
         return fail(ST_ERR_UNSUPPORTED, std::string("implicit solve: ") + why);
-    if (any) {
-        int rc = alloc_s(&x->wake_mask_d, (size_t)nic);
-        if (rc == ST_OK) rc = alloc_s(&x->wpart, (size_t)nic * NWS * x->nq * x->nq);
+    for (int f = 0; f < NFAM; f++) {
+        x->pmask[f] = m[f];
+        x->pfam_on[f] = on[f] != 0;
+        if (!on[f]) continue;
+        const size_t len = (size_t)fam_len(f, nic, njc);
+        int rc = alloc_s(&x->pmask_d[f], len);
+        if (rc == ST_OK) rc = alloc_s(&x->wpart[f], len * NWS * x->nq * x->nq);
         if (rc) return rc;
-        ST_CUDA(cudaMemcpyAsync(x->wake_mask_d, m.data(), nic * sizeof(int), cudaMemcpyHostToDevice, x->stream));
-        ST_CUDA(cudaStreamSynchronize(x->stream));
+        ST_CUDA(cudaMemcpyAsync(x->pmask_d[f], m[f].data(), len * sizeof(int), cudaMemcpyHostToDevice, x->stream));
+        x->has_partners = true;
     }
-    x->wake_cols = m;
-    x->has_wake = any != 0;
-    x->wake_checked = true;
+    ST_CUDA(cudaStreamSynchronize(x->stream));
+    x->partners_checked = true;
     return ST_OK;
 }
 
-// Wake partner blocks of the order-`order` residual into x->wpart
-// (2 halves x 3 residues x nq JVPs).
-int assemble_wake(st_ctx* x, int order) {
+// Partner blocks of the order-`order` residual into x->wpart[f]: per family,
+// residue k and component, a full and a frozen JVP of the same seed (x->kz ->
+// x->kw, x->kr; both free during assembly).
+int assemble_partners(st_ctx* x, int order) {
     const int nq = x->nq, nic = x->c.ni - 1, njc = x->c.nj - 1;
     cudaStream_t s = x->stream;
-    ST_CUDA(cudaMemsetAsync(x->wpart, 0, (size_t)nic * NWS * nq * nq * 8, s));
-    const unsigned g = grid_for(x->ncell), gw = grid_for((size_t)nic * NWS);
-    for (int side = 0; side < 2; side++)
+    for (int f = 0; f < NFAM; f++) {
+        if (!x->pfam_on[f]) continue;
+        const int len = fam_len(f, nic, njc);
+        const unsigned gl = grid_for((size_t)len), gw = grid_for((size_t)len * NWS);
+        ST_CUDA(cudaMemsetAsync(x->wpart[f], 0, (size_t)len * NWS * nq * nq * 8, s));
         for (int k = 0; k < 3; k++) {
             bool seeded = false;
-            for (int i = 0; i < nic; i++) seeded |= x->wake_cols[i] && wake_side(i, nic) == side && i % 3 == k;
+            for (int b = k; b < len; b += 3) seeded |= x->pmask[f][b] != 0;
             if (!seeded) continue;
             for (int comp = 0; comp < nq; comp++) {
-                if (nq == 5) k_wake_seed<5><<<g, 256, 0, s>>>(nic, njc, x->wake_mask_d, side, k, comp, x->kz);
-                else k_wake_seed<4><<<g, 256, 0, s>>>(nic, njc, x->wake_mask_d, side, k, comp, x->kz);
+                ST_CUDA(cudaMemsetAsync(x->kz, 0, x->ncell * nq * 8, s));
+                if (nq == 5) k_partner_seed<5><<<gl, 256, 0, s>>>(f, nic, njc, x->pmask_d[f], k, comp, x->kz);
+                else k_partner_seed<4><<<gl, 256, 0, s>>>(f, nic, njc, x->pmask_d[f], k, comp, x->kz);
                 int rc = stx::run_jvp(x, x->kz, nullptr, x->kw, order, 0);
+                if (rc == ST_OK) rc = stx::run_jvp(x, x->kz, nullptr, x->kr, order, 1);
                 if (rc) return rc;
-                if (nq == 5) k_wake_extract<5><<<gw, 256, 0, s>>>(nic, njc, x->wake_mask_d, side, k, comp, x->kw, x->wpart);
-                else k_wake_extract<4><<<gw, 256, 0, s>>>(nic, njc, x->wake_mask_d, side, k, comp, x->kw, x->wpart);
+                if (nq == 5)
+                    k_partner_extract<5><<<gw, 256, 0, s>>>(f, nic, njc, x->pmask_d[f], k, comp, x->kw, x->kr, x->wpart[f]);
+                else
+                    k_partner_extract<4><<<gw, 256, 0, s>>>(f, nic, njc, x->pmask_d[f], k, comp, x->kw, x->kr, x->wpart[f]);
             }
         }
-    ST_LAUNCH_CHECK("wake partner assembly");
+    }
+    ST_LAUNCH_CHECK("partner assembly");
     return ST_OK;
 }
 
@@ -730,7 +740,7 @@ int assemble_into(st_ctx* x, int order, double* out) {
             for (int comp = 0; comp < nq; comp++) {
                 if (nq == 5) k_seed<5><<<g, 256, 0, s>>>(nic, njc, cs, ci, cj, comp, x->kz);
                 else k_seed<4><<<g, 256, 0, s>>>(nic, njc, cs, ci, cj, comp, x->kz);
-                int rc = stx::run_jvp(x, x->kz, nullptr, x->kw, order, x->has_wake ? 1 : 0);
+                int rc = stx::run_jvp(x, x->kz, nullptr, x->kw, order, x->has_partners ? 1 : 0);
                 if (rc) return rc;
                 if (nq == 5) k_extract<5><<<g, 256, 0, s>>>(nic, njc, cs, ci, cj, comp, x->kw, out);
                 else k_extract<4><<<g, 256, 0, s>>>(nic, njc, cs, ci, cj, comp, x->kw, out);
@@ -739,18 +749,18 @@ int assemble_into(st_ctx* x, int order, double* out) {
     return ST_OK;
 }
 
-// The operator's Jacobian: regular blocks and, with a wake cut, its partners.
+// The operator's Jacobian: regular blocks and the non-local copies' partners.
 int assemble(st_ctx* x, int order) {
-    int rc = wake_setup(x);
+    int rc = partner_setup(x);
     if (rc == ST_OK) rc = ensure_solver(x, 1);
     if (rc == ST_OK) rc = assemble_into(x, order, x->jac);
-    if (rc == ST_OK && x->has_wake) rc = assemble_wake(x, order);
+    if (rc == ST_OK && x->has_partners) rc = assemble_partners(x, order);
     return rc;
 }
 
 // Operator Jacobian (order `order`) and, for the preconditioner, the
 // first-order Jacobian (reusing the operator when it is first order).  The
-// preconditioner keeps the regular blocks only: the wake partners lie
+// preconditioner keeps the regular blocks only: the partner blocks lie
 // outside the ILU(0) pattern.
 int assemble_pair(st_ctx* x, int order) {
     int rc = assemble(x, order);
@@ -781,14 +791,16 @@ int apply_A(st_ctx* x, const LinOp& op, const double* in, double* out) {
         if (op.trans) k_spmv<4, true><<<g, 256, 0, x->stream>>>(nic, njc, x->jac, in, out, op.dt, op.sd, op.sj);
         else k_spmv<4, false><<<g, 256, 0, x->stream>>>(nic, njc, x->jac, in, out, op.dt, op.sd, op.sj);
     }
-    if (x->has_wake) {
-        const unsigned gw = grid_for((size_t)nic);
+    for (int f = 0; f < NFAM; f++) {
+        if (!x->pfam_on[f]) continue;
+        const unsigned gl = grid_for((size_t)fam_len(f, nic, njc));
+        const double* W = x->wpart[f];
         if (x->nq == 5) {
-            if (op.trans) k_wake_apply<5, true><<<gw, 256, 0, x->stream>>>(nic, njc, x->wpart, in, out, op.sj);
-            else k_wake_apply<5, false><<<gw, 256, 0, x->stream>>>(nic, njc, x->wpart, in, out, op.sj);
+            if (op.trans) k_partner_apply<5, true><<<gl, 256, 0, x->stream>>>(f, nic, njc, W, in, out, op.sj);
+            else k_partner_apply<5, false><<<gl, 256, 0, x->stream>>>(f, nic, njc, W, in, out, op.sj);
         } else {
-            if (op.trans) k_wake_apply<4, true><<<gw, 256, 0, x->stream>>>(nic, njc, x->wpart, in, out, op.sj);
-            else k_wake_apply<4, false><<<gw, 256, 0, x->stream>>>(nic, njc, x->wpart, in, out, op.sj);
+            if (op.trans) k_partner_apply<4, true><<<gl, 256, 0, x->stream>>>(f, nic, njc, W, in, out, op.sj);
+            else k_partner_apply<4, false><<<gl, 256, 0, x->stream>>>(f, nic, njc, W, in, out, op.sj);
         }
     }
     ST_LAUNCH_CHECK("spmv");
@@ -948,7 +960,7 @@ extern "C" {
 
 int st_jacobian_assemble(st_ctx* x, int lhs) {
     if (!x) return fail(ST_ERR_ARG, "st_jacobian_assemble: null context");
-    if (int rc0 = wake_setup(x)) return rc0;
+    if (int rc0 = partner_setup(x)) return rc0;
     int rc = assemble_pair(x, lhs ? x->c.lhs_order : x->c.order);
     if (rc) return rc;
     ST_CUDA(cudaStreamSynchronize(x->stream));
@@ -991,7 +1003,7 @@ int st_solve(st_ctx* x, const st_solve_params* p, st_solve_stats* stats, double*
              int* steps_done) {
     if (!x || !p) return fail(ST_ERR_ARG, "st_solve: null argument");
     if (p->max_steps < 0 || p->krylov_m < 1 || p->krylov_m > 500) return fail(ST_ERR_ARG, "st_solve: bad parameters");
-    if (int rc0 = wake_setup(x)) return rc0;
+    if (int rc0 = partner_setup(x)) return rc0;
     int rc = ensure_solver(x, p->krylov_m);
     if (rc) return rc;
     const int nq = x->nq;
@@ -1175,7 +1187,7 @@ int st_adjoint_solve_device(st_ctx* x, const double* b_dev, double* psi_dev, dou
                             double rtol, st_solve_stats* stats) {
     if (!x || !b_dev || !psi_dev) return fail(ST_ERR_ARG, "st_adjoint_solve_device: null argument");
     if (krylov_m < 1 || krylov_m > 500 || maxit < 1) return fail(ST_ERR_ARG, "st_adjoint_solve_device: krylov sizes");
-    if (int rc0 = wake_setup(x)) return rc0;
+    if (int rc0 = partner_setup(x)) return rc0;
     // exact Jacobian of the residual actually solved (order, not lhs_order)
     int rc = assemble_pair(x, x->c.order);
     if (rc) return rc;
@@ -1193,7 +1205,7 @@ int st_tangent_solve_device(st_ctx* x, const double* b_dev, double* dq_dev, doub
                             double rtol, st_solve_stats* stats) {
     if (!x || !b_dev || !dq_dev) return fail(ST_ERR_ARG, "st_tangent_solve_device: null argument");
     if (krylov_m < 1 || krylov_m > 500 || maxit < 1) return fail(ST_ERR_ARG, "st_tangent_solve_device: krylov sizes");
-    if (int rc0 = wake_setup(x)) return rc0;
+    if (int rc0 = partner_setup(x)) return rc0;
     int rc = assemble_pair(x, x->c.order);
     if (rc) return rc;
     rc = stx::run_dt(x, cfl_prec);

@@ -1,65 +1,84 @@
 """The implicit solver's block Jacobian restated in numpy over the oracle's
 exact JVPs (test infrastructure; the product assembles on the GPU,
-structured_gb300/csrc/st_solver.cu).
+structured_gb300/csrc/st_solver.cu and st_partner.cuh).
 
 Layout, as on the device:
 - regular blocks ``[nic][njc][13][nq][nq]`` for the 13-point stencil offsets
   OFFSETS, assembled from JVPs over a 5x5 (second order) or 3x3 (first order)
-  cell colouring, with the wake ghosts' tangents held at zero so that the
-  colouring sees only local dependencies;
-- wake partner blocks ``[nic][4][nq][nq]``: the wake cut (bc.cpp:224-263)
-  makes the bottom ghost below column a a copy of cell (nic-1-a, 0), and that
-  ghost reaches rows (a-1, 0), (a, 0), (a+1, 0) and (a, 1).  Slot t of row
-  column i holds d R(i, j_t) / d q(nic-1-(i-d_t), 0) for SLOTS[t] = (j_t, d_t).
-  They are assembled by seeding the row-0 source cells of one half of the grid
-  whose column is congruent to k mod 3 (ghost windows three columns apart
-  never share a row), and reading the rows next to their mirror ghosts on the
-  other half, where the seeds have no local effect."""
+  cell colouring, with the tangents of the non-local boundary copies (wake
+  cut, periodic) held at zero so that the colouring sees only local
+  dependencies;
+- partner blocks per family of copied ghosts, ``[line length][4][nq][nq]``:
+  FAM_WAKE (bc.cpp:224-263: the bottom ghost below column b copies cell
+  (nic-1-b, 0)), FAM_LEFT and FAM_RIGHT (bc.cpp:329-365: the ghost left of
+  row b copies cell (nic-1, b), the one right of it cell (0, b)).  Ghost b
+  reaches the rows at line positions b-1, b, b+1 next to its boundary and the
+  row at b one further in; slot t of line position p holds the block of row
+  fam_row(f, p, t) against the source of ghost p - SLOTS[t][1].  A partner pass
+  seeds the sources of the ghosts b = k mod 3 of one family and keeps the
+  difference of a full and a frozen JVP: the part the copies carry."""
 from __future__ import annotations
 
 import numpy as np
 
 OFFSETS = ((0, 0), (-1, 0), (1, 0), (0, -1), (0, 1), (-2, 0), (2, 0), (0, -2), (0, 2),
            (-1, -1), (-1, 1), (1, -1), (1, 1))
-SLOTS = ((0, -1), (0, 0), (0, 1), (1, 0))
-MIN_SIDE_GAP = 6
+SLOTS = ((0, -1), (0, 0), (0, 1), (1, 0))  # (distance from the boundary, row position - ghost position)
+FAM_WAKE, FAM_LEFT, FAM_RIGHT = 0, 1, 2
 
 
-def wake_columns(c) -> np.ndarray:
-    """Mask of the columns whose bottom ghost is a wake copy (both halves of
-    each bottom wake range, padded start..end -> columns start-1..end-1 and
-    nic-end..nic-start)."""
-    nic = c.ni - 1
-    m = np.zeros(nic, dtype=bool)
+def fam_len(f, nic, njc):
+    return nic if f == FAM_WAKE else njc
+
+
+def fam_row(f, p, t, nic):
+    l = SLOTS[t][0]
+    if f == FAM_WAKE:
+        return p, l
+    return (l, p) if f == FAM_LEFT else (nic - 1 - l, p)
+
+
+def fam_src(f, b, nic):
+    if f == FAM_WAKE:
+        return nic - 1 - b, 0
+    return (nic - 1, b) if f == FAM_LEFT else (0, b)
+
+
+def partner_masks(c):
+    """Ghost masks of the non-local copies and which families occur; ValueError
+    for the boundary lists the layout cannot hold."""
+    nic, njc = c.ni - 1, c.nj - 1
+    masks = [np.zeros(nic, dtype=bool), np.zeros(njc, dtype=bool), np.zeros(njc, dtype=bool)]
+    on = [False, False, False]
     for b in c.boundaries:
-        if b.type != "wake":
+        if b.type not in ("wake", "periodic"):
             continue
-        if b.face != "bottom":
-            raise ValueError("wake cut on the %s face" % b.face)
-        end = b.end if b.end >= 0 else nic + 2 + b.end
-        if b.start < 1:
-            raise ValueError("wake range starts on the corner ghost")
-        for ip in range(b.start, end + 1):
-            m[ip - 1] = True
-            m[nic - ip] = True
-    return m
-
-
-def side_of(i: int, nic: int) -> int:
-    return 1 if 2 * i > nic - 1 else 0
-
-
-def check_sides(mask: np.ndarray) -> None:
-    """The two halves of the cut must be apart: a seed's own stencil (two
-    columns) never reaches the rows next to another seed's mirror ghost."""
-    nic = mask.size
-    cols = np.nonzero(mask)[0]
-    if cols.size == 0:
-        return
-    left = [i for i in cols if side_of(i, nic) == 0]
-    right = [i for i in cols if side_of(i, nic) == 1]
-    if not left or not right or min(right) - max(left) < MIN_SIDE_GAP:
-        raise ValueError("wake halves closer than %d columns" % MIN_SIDE_GAP)
+        bt = b.face in ("bottom", "top")
+        end = b.end if b.end >= 0 else (nic if bt else njc) + 2 + b.end
+        if b.start > end:
+            continue
+        if b.type == "wake":
+            if b.face != "bottom":
+                raise ValueError("wake cut on the %s face" % b.face)
+            if b.start < 1 or end > nic:
+                raise ValueError("wake range on a corner ghost")
+            for ip in range(b.start, end + 1):
+                masks[FAM_WAKE][ip - 1] = True
+                masks[FAM_WAKE][nic - ip] = True
+            on[FAM_WAKE] = True
+        else:
+            if bt:
+                raise ValueError("periodic boundaries on the %s face" % b.face)
+            if b.start > 1 or end < njc:
+                raise ValueError("periodic range not covering every row")
+            masks[FAM_LEFT][:] = True
+            masks[FAM_RIGHT][:] = True
+            on[FAM_LEFT] = on[FAM_RIGHT] = True
+    if on[FAM_WAKE] and on[FAM_LEFT]:
+        raise ValueError("a wake cut together with periodic boundaries")
+    if (on[FAM_WAKE] or on[FAM_LEFT]) and (nic < 2 or njc < 2):
+        raise ValueError("fewer than two cells across")
+    return masks, on
 
 
 def assemble_regular(port, q, order: int, freeze: bool = True) -> np.ndarray:
@@ -68,7 +87,7 @@ def assemble_regular(port, q, order: int, freeze: bool = True) -> np.ndarray:
     half = cs // 2
     jac = np.zeros((nic, njc, len(OFFSETS), nq, nq))
     ii, jj = np.meshgrid(np.arange(nic), np.arange(njc), indexing="ij")
-    port.freeze_wake(freeze)
+    port.freeze_nonlocal(freeze)
     try:
         for ci in range(cs):
             for cj in range(cs):
@@ -87,36 +106,58 @@ def assemble_regular(port, q, order: int, freeze: bool = True) -> np.ndarray:
                         sel &= (ic >= 0) & (ic < nic) & (jc >= 0) & (jc < njc)
                         jac[sel, o, :, comp] = jv[sel]
     finally:
-        port.freeze_wake(False)
+        port.freeze_nonlocal(False)
     return jac
 
 
-def assemble_partners(port, q, mask: np.ndarray, order: int) -> np.ndarray:
+def assemble_partners(port, q, masks, on, order: int):
+    """Partner blocks per family (None where the family is absent)."""
     nic, njc, nq = q.shape
-    W = np.zeros((nic, len(SLOTS), nq, nq))
-    for side in (0, 1):
+    W = [None, None, None]
+    for f in range(3):
+        if not on[f]:
+            continue
+        n = fam_len(f, nic, njc)
+        Wf = np.zeros((n, len(SLOTS), nq, nq))
         for k in range(3):
-            seeds = [s for s in range(nic) if mask[s] and side_of(s, nic) == side and s % 3 == k]
-            if not seeds:
+            ghosts = [b for b in range(k, n, 3) if masks[f][b]]
+            if not ghosts:
                 continue
             for comp in range(nq):
                 v = np.zeros_like(q)
-                v[seeds, 0, comp] = 1.0
-                jv = port.jvp(q, v, lhs=(order == 1))
-                for i in range(nic):
-                    for t, (j, d) in enumerate(SLOTS):
-                        a = i - d
-                        if a < 0 or a >= nic or not mask[a]:
-                            continue
-                        src = nic - 1 - a
-                        if side_of(src, nic) != side or src % 3 != k:
-                            continue
-                        W[i, t, :, comp] = jv[i, j]
+                for b in ghosts:
+                    v[fam_src(f, b, nic) + (comp,)] = 1.0
+                full = port.jvp(q, v, lhs=(order == 1))
+                port.freeze_nonlocal(True)
+                try:
+                    frozen = port.jvp(q, v, lhs=(order == 1))
+                finally:
+                    port.freeze_nonlocal(False)
+                for p in range(n):
+                    for t, (l, d) in enumerate(SLOTS):
+                        b = p - d
+                        if 0 <= b < n and masks[f][b] and b % 3 == k:
+                            r = fam_row(f, p, t, nic)
+                            Wf[p, t, :, comp] = full[r] - frozen[r]
+        W[f] = Wf
     return W
 
 
+def _partner_terms(W, nic, njc):
+    """(row cell, source cell, block) of every partner block."""
+    for f in range(3):
+        if W is None or W[f] is None:
+            continue
+        n = fam_len(f, nic, njc)
+        for p in range(n):
+            for t, (l, d) in enumerate(SLOTS):
+                b = p - d
+                if 0 <= b < n:
+                    yield fam_row(f, p, t, nic), fam_src(f, b, nic), W[f][p, t]
+
+
 def apply(jac, W, x, trans: bool = False) -> np.ndarray:
-    """J x (or J^T x) from the regular blocks and the wake partners."""
+    """J x (or J^T x) from the regular blocks and the partner blocks."""
     nic, njc, nq = x.shape
     y = np.zeros_like(x)
     for o, (oi, oj) in enumerate(OFFSETS):
@@ -132,42 +173,35 @@ def apply(jac, W, x, trans: bool = False) -> np.ndarray:
                     y[ic, jc] += jac[i, j, o].T @ x[i, j]
                 else:
                     y[i, j] += jac[i, j, o] @ x[ic, jc]
-    if W is not None:
-        for i in range(nic):
-            for t, (j, d) in enumerate(SLOTS):
-                a = i - d
-                if a < 0 or a >= nic:
-                    continue
-                pc = nic - 1 - a
-                if trans:
-                    y[pc, 0] += W[i, t].T @ x[i, j]
-                else:
-                    y[i, j] += W[i, t] @ x[pc, 0]
+    for r, src, w in _partner_terms(W, nic, njc):
+        if trans:
+            y[src] += w.T @ x[r]
+        else:
+            y[r] += w @ x[src]
     return y
 
 
 def to_sparse(jac, W):
-    """The same operator as a scipy CSR matrix over (i*njc + j)*nq + k."""
+    """The same operator as a scipy CSR matrix over (i*njc + j)*nq + k
+    (duplicate entries are summed)."""
     import scipy.sparse as sp
     nic, njc, noff, nq, _ = jac.shape
     rows, cols, vals = [], [], []
     kk, ll = np.meshgrid(np.arange(nq), np.arange(nq), indexing="ij")
-    for i in range(nic):
-        for j in range(njc):
-            r0 = (i * njc + j) * nq
-            for o, (oi, oj) in enumerate(OFFSETS):
-                ic, jc = i + oi, j + oj
-                if 0 <= ic < nic and 0 <= jc < njc:
-                    rows.append(r0 + kk.ravel()); cols.append((ic * njc + jc) * nq + ll.ravel())
-                    vals.append(jac[i, j, o].ravel())
-    if W is not None:
-        for i in range(nic):
-            for t, (j, d) in enumerate(SLOTS):
-                a = i - d
-                if 0 <= a < nic and np.any(W[i, t]):
-                    r0 = (i * njc + j) * nq
-                    rows.append(r0 + kk.ravel()); cols.append(((nic - 1 - a) * njc) * nq + ll.ravel())
-                    vals.append(W[i, t].ravel())
+    ii, jj = np.meshgrid(np.arange(nic), np.arange(njc), indexing="ij")
+    for o, (oi, oj) in enumerate(OFFSETS):
+        ic, jc = ii + oi, jj + oj
+        ok = (ic >= 0) & (ic < nic) & (jc >= 0) & (jc < njc)
+        r0 = ((ii * njc + jj) * nq)[ok]
+        c0 = ((ic * njc + jc) * nq)[ok]
+        rows.append((r0[:, None] + kk.ravel()[None, :]).ravel())
+        cols.append((c0[:, None] + ll.ravel()[None, :]).ravel())
+        vals.append(jac[:, :, o][ok].reshape(-1, nq * nq).ravel())
+    for (ri, rj), (si, sj), w in _partner_terms(W, nic, njc):
+        if np.any(w):
+            rows.append((ri * njc + rj) * nq + kk.ravel())
+            cols.append((si * njc + sj) * nq + ll.ravel())
+            vals.append(w.ravel())
     n = nic * njc * nq
     return sp.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))), shape=(n, n))
 
@@ -175,15 +209,12 @@ def to_sparse(jac, W):
 def steady_newton(port, c, q, cfl=1.0, growth=1.5, cfl_max=1e8, max_rel_drho=0.2, tol=1e-10, max_steps=80):
     """Steady state of the oracle's residual by pseudo-time Newton: each step
     solves (I/dt - J) dq = R, the implicit solver's system, exactly (sparse LU
-    of the full second-order Jacobian with the wake partners), damped so that
+    of the full second-order Jacobian with the partner blocks), damped so that
     no density changes by more than ``max_rel_drho``; CFL grows by ``growth``
     per step.  Returns the state and the max-over-components L2 norms."""
     import scipy.sparse as sp
     import scipy.sparse.linalg as spla
-    mask = wake_columns(c)
-    has_wake = bool(mask.any())
-    if has_wake:
-        check_sides(mask)
+    masks, on = partner_masks(c)
     q = q.copy()
     hist = []
     for _ in range(max_steps):
@@ -192,7 +223,7 @@ def steady_newton(port, c, q, cfl=1.0, growth=1.5, cfl_max=1e8, max_rel_drho=0.2
         if not np.isfinite(hist[-1]) or hist[-1] < tol:
             break
         jac = assemble_regular(port, q, 2)
-        W = assemble_partners(port, q, mask, 2) if has_wake else None
+        W = assemble_partners(port, q, masks, on, 2)
         M = sp.diags(1.0 / port.dt(q, cfl).ravel()) - to_sparse(jac, W)
         dq = spla.spsolve(M.tocsc(), R.ravel()).reshape(q.shape)
         rel = np.abs(dq[..., 0] / q[..., 0]).max()

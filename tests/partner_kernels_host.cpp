@@ -1,0 +1,49 @@
+// Host build of structured_gb300/csrc/st_partner.cuh (test infrastructure):
+// the same kernel source compiled by g++, each launch run serially as one
+// block of one thread, so that the CPU tests can check the ghost masks, the
+// partner seeds and extraction, and the partner products against the oracle
+// and catch any index outside its buffer.
+#define __global__
+#define __device__
+#define __host__
+struct HostDim3 {
+    int x;
+};
+static const HostDim3 blockIdx{0}, threadIdx{0}, blockDim{1}, gridDim{1};
+
+#include "../structured_gb300/csrc/st_partner.cuh"
+
+using namespace st;
+
+extern "C" {
+
+int ph_slots() { return NWS; }
+
+int ph_masks(int nic, int njc, const st_bc* bcs, int nbc, int* mask_wake, int* mask_left, int* mask_right,
+             int* on) {
+    const char* why = "";
+    return partner_masks(nic, njc, bcs, nbc, mask_wake, mask_left, mask_right, on, &why);
+}
+
+void ph_seed(int nq, int f, int nic, int njc, const int* mask, int k, int comp, double* v) {
+    if (nq == 5) k_partner_seed<5>(f, nic, njc, mask, k, comp, v);
+    else k_partner_seed<4>(f, nic, njc, mask, k, comp, v);
+}
+
+void ph_extract(int nq, int f, int nic, int njc, const int* mask, int k, int comp, const double* jv_full,
+                const double* jv_frozen, double* W) {
+    if (nq == 5) k_partner_extract<5>(f, nic, njc, mask, k, comp, jv_full, jv_frozen, W);
+    else k_partner_extract<4>(f, nic, njc, mask, k, comp, jv_full, jv_frozen, W);
+}
+
+void ph_apply(int nq, int trans, int f, int nic, int njc, const double* W, const double* x, double* y, double sj) {
+    if (nq == 5) {
+        if (trans) k_partner_apply<5, true>(f, nic, njc, W, x, y, sj);
+        else k_partner_apply<5, false>(f, nic, njc, W, x, y, sj);
+    } else {
+        if (trans) k_partner_apply<4, true>(f, nic, njc, W, x, y, sj);
+        else k_partner_apply<4, false>(f, nic, njc, W, x, y, sj);
+    }
+}
+
+}  // extern "C"

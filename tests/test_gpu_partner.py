@@ -1,10 +1,10 @@
-"""The implicit solver across the wake cut of a NACA 0012 C-grid on the GPU
-(bc.cpp:224-263 couples cell (a, 0) to the ghost below column nic-1-a):
-the assembled operator (regular blocks + wake partners) against the GPU's own
-JVP/VJP, its regular blocks against the oracle's frozen-wake colouring, and
-the pseudo-time Newton steady state against the oracle's (sparse LU Newton
-on the exact Jacobian, tests/block_jacobian.py) with Cl/Cd from the surface
-output."""
+"""The implicit solver across non-local boundary copies on the GPU: the wake
+cut of a NACA 0012 C-grid (bc.cpp:224-263) and the periodic channel
+(bc.cpp:329-365).  The assembled operator (regular blocks + partner blocks)
+against the GPU's own JVP/VJP, its regular blocks against the oracle's frozen
+colouring, and the pseudo-time Newton steady states against the oracle's
+(sparse LU Newton on the exact Jacobian, tests/block_jacobian.py), with Cl/Cd
+from the surface output for the airfoil."""
 import numpy as np
 import pytest
 
@@ -20,16 +20,27 @@ def naca(tmp_path, turbulence="none", ni=41, nj=9, tail=11):
     return c, C.load_grid(c)
 
 
+def channel(tmp_path, ni=3, nj=21, turbulence="none"):
+    c = C.channel_case(str(tmp_path), "ch", nj=nj, ni=ni)
+    c.turbulence = turbulence
+    c.lhs_order = 1
+    return c, C.load_grid(c)
+
+
 def rel(a, b):
     return float(np.abs(a - b).max() / (np.abs(b).max() + 1e-300))
 
 
+@pytest.mark.parametrize("which", ["naca", "channel2", "channel6"])
 @pytest.mark.parametrize("turb", ["none", "sa"])
 @pytest.mark.parametrize("lhs", [False, True])
-def test_wake_operator_matches_jvp_and_vjp(gpu_lib, tmp_path, turb, lhs):
+def test_partner_operator_matches_jvp_and_vjp(gpu_lib, tmp_path, which, turb, lhs):
     import torch
     from structured_gb300.solver import EulerEquation
-    c, (xv, yv) = naca(tmp_path, turb)
+    if which == "naca":
+        c, (xv, yv) = naca(tmp_path, turb)
+    else:
+        c, (xv, yv) = channel(tmp_path, ni=3 if which == "channel2" else 7, turbulence=turb)
     q = C.perturbed_state(c, 41)
     eq = EulerEquation(c, xv, yv)
     eq.set_state(q)
@@ -51,10 +62,11 @@ def test_wake_operator_matches_jvp_and_vjp(gpu_lib, tmp_path, turb, lhs):
     assert rel(jt.cpu().numpy(), oq) < 1e-11
 
 
-def test_wake_regular_blocks_match_oracle_colouring(gpu_lib, port_built, tmp_path):
+@pytest.mark.parametrize("which", ["naca", "channel2"])
+def test_regular_blocks_match_oracle_colouring(gpu_lib, port_built, tmp_path, which):
     from oracle.port import PortCase
     from structured_gb300.solver import EulerEquation
-    c, (xv, yv) = naca(tmp_path, "sa")
+    c, (xv, yv) = naca(tmp_path, "sa") if which == "naca" else channel(tmp_path, turbulence="sa")
     q = C.perturbed_state(c, 43)
     eq = EulerEquation(c, xv, yv)
     eq.set_state(q)
@@ -94,12 +106,40 @@ def test_wake_cut_newton_matches_oracle_steady_state(gpu_lib, port_built, tmp_pa
     assert f_ref["cd_viscous"] > 0 and f_ref["cd_pressure"] > 0
 
 
+def test_periodic_channel_newton_matches_oracle_steady_state(gpu_lib, port_built, tmp_path):
+    """The reference's implicit channel example (examples/laminar/channel/
+    implicit.inp: periodic in x, isothermal walls, body force) on 3 x 41."""
+    from oracle.port import PortCase
+    from structured_gb300.solver import EulerEquation, Solver
+    c, (xv, yv) = channel(tmp_path, nj=41)
+    c.lhs_order = 2
+    q0 = C.freestream_state(c)
+    eq = EulerEquation(c, xv, yv)
+    eq.set_state(q0)
+    # the residual's round-off floor here is ~1e-11 (1e-12 of the first one)
+    ok, hist = Solver(eq, max_steps=100, cfl=10.0, cfl_ramp=0, cfl_growth=2.0, max_rel_drho=0.2, tolerance=1e-10,
+                      krylov_m=80, krylov_maxit=400, krylov_rtol=1e-8).solve()
+    assert ok, hist[-3:]
+    q_ref, h_ref = BJ.steady_newton(PortCase(c, xv, yv), c, q0, cfl=10.0, growth=2.0, tol=3e-11)
+    assert h_ref[-1] < 3e-11
+    q_gpu = eq.get_state()
+    scale = np.abs(q_ref).max(axis=(0, 1))
+    assert (np.abs(q_gpu - q_ref).max(axis=(0, 1)) / scale).max() < 1e-8
+
+
 def test_refused_boundary_lists(gpu_lib, tmp_path):
     from structured_gb300.solver import EulerEquation, StructuredError
     c, (xv, yv) = naca(tmp_path)
-    c.boundaries[3].end = 18          # the halves five columns apart
+    c.boundaries[3].face = "top"      # the kernel copies it, the implicit layout does not
     eq = EulerEquation(c, xv, yv)
     eq.set_state(C.freestream_state(c))
+    with pytest.raises(StructuredError) as e:
+        eq.jacobian_assemble()
+    assert e.value.code == -6
+    ch, (xv, yv) = channel(tmp_path)
+    ch.boundaries[2].face = "bottom"  # periodic in j
+    eq = EulerEquation(ch, xv, yv)
+    eq.set_state(C.freestream_state(ch))
     with pytest.raises(StructuredError) as e:
         eq.jacobian_assemble()
     assert e.value.code == -6

@@ -1,0 +1,316 @@
+"""Non-local boundary copies in the implicit solver's Jacobian, on CPU against
+the oracle: the wake cut of a NACA 0012 C-grid (bc.cpp:224-263) and the
+periodic channel (bc.cpp:329-365).  Where their coupling lands, the block
+layout the GPU assembles (regular 13-point blocks from a frozen colouring plus
+four partner slots per ghost, tests/block_jacobian.py) reproducing the
+oracle's exact JVP and VJP, Newton on it converging superlinearly, and the
+device source of the partner pass (structured_gb300/csrc/st_partner.cuh,
+compiled for the host by tests/partner_kernels_host.cpp) matching the numpy
+layout without touching memory outside its buffers."""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import block_jacobian as BJ
+from structured_gb300 import case as C
+
+VARIANTS = [("none", "roe", 2), ("sa", "roe", 2), ("none", "ausm", 2), ("none", "roe", 1), ("sa", "roe", 1)]
+
+
+def naca(tmp_path, turbulence="none", flux="roe", ni=41, nj=9, tail=11):
+    from oracle.port import PortCase
+    c = C.naca0012_case(str(tmp_path), "naca", ni=ni, nj=nj, tail=tail)
+    c.turbulence, c.flux = turbulence, flux
+    xv, yv = C.load_grid(c)
+    return c, PortCase(c, xv, yv)
+
+
+def channel(tmp_path, ni=3, nj=11, turbulence="none", flux="roe"):
+    from oracle.port import PortCase
+    c = C.channel_case(str(tmp_path), "ch", nj=nj, ni=ni)
+    c.turbulence, c.flux = turbulence, flux
+    c.lhs_order = 1  # lhs=True evaluates the first-order residual, as in the NACA case
+    xv, yv = C.load_grid(c)
+    return c, PortCase(c, xv, yv)
+
+
+def dense_blocks(port, q, order):
+    """max |entry| of every (row cell, column cell) block of the Jacobian."""
+    nic, njc, nq = q.shape
+    B = np.zeros((nic, njc, nic, njc))
+    for i in range(nic):
+        for j in range(njc):
+            for k in range(nq):
+                v = np.zeros_like(q)
+                v[i, j, k] = 1.0
+                B[:, :, i, j] = np.maximum(B[:, :, i, j], np.abs(port.jvp(q, v, lhs=(order == 1))).max(axis=2))
+    return B
+
+
+def off_stencil(B):
+    out = []
+    for ri, rj, ci, cj in zip(*np.nonzero(B)):
+        if (ci - ri, cj - rj) not in BJ.OFFSETS:
+            out.append((int(ri), int(rj), int(ci), int(cj)))
+    return out
+
+
+def copy_part(port, q, order):
+    """(row cell, column cell) pairs where the full and the frozen Jacobian differ."""
+    nic, njc, nq = q.shape
+    out = set()
+    for i in range(nic):
+        for j in range(njc):
+            for k in range(nq):
+                v = np.zeros_like(q)
+                v[i, j, k] = 1.0
+                full = port.jvp(q, v, lhs=(order == 1))
+                port.freeze_nonlocal(True)
+                try:
+                    frozen = port.jvp(q, v, lhs=(order == 1))
+                finally:
+                    port.freeze_nonlocal(False)
+                for ri, rj in zip(*np.nonzero(np.abs(full - frozen).max(axis=2))):
+                    out.add(((int(ri), int(rj)), (i, j)))
+    return out
+
+
+def slot_pairs(c, nic, njc):
+    masks, on = BJ.partner_masks(c)
+    pairs = set()
+    for f in range(3):
+        if not on[f]:
+            continue
+        n = BJ.fam_len(f, nic, njc)
+        for p in range(n):
+            for t, (l, d) in enumerate(BJ.SLOTS):
+                b = p - d
+                if 0 <= b < n and masks[f][b]:
+                    pairs.add((BJ.fam_row(f, p, t, nic), BJ.fam_src(f, b, nic)))
+    return pairs
+
+
+@pytest.mark.parametrize("which,turbulence,order", [("naca", "none", 2), ("naca", "sa", 2), ("naca", "none", 1),
+                                                     ("channel2", "none", 2), ("channel6", "sa", 2),
+                                                     ("channel6", "none", 1)])
+def test_copy_coupling_lands_in_the_partner_slots(port_built, tmp_path, which, turbulence, order):
+    if which == "naca":
+        c, port = naca(tmp_path, turbulence)
+    else:
+        c, port = channel(tmp_path, ni=3 if which == "channel2" else 7, turbulence=turbulence)
+    q = C.perturbed_state(c, 7)
+    nic, njc, _ = q.shape
+    part = copy_part(port, q, order)
+    assert part
+    assert part <= slot_pairs(c, nic, njc)
+    # with the copies frozen only the 13-point stencil is left
+    port.freeze_nonlocal(True)
+    try:
+        assert off_stencil(dense_blocks(port, q, order)) == []
+    finally:
+        port.freeze_nonlocal(False)
+
+
+def products_match(c, port, q, order):
+    masks, on = BJ.partner_masks(c)
+    jac = BJ.assemble_regular(port, q, order)
+    W = BJ.assemble_partners(port, q, masks, on, order)
+    x = np.random.default_rng(3).standard_normal(q.shape)
+    jv = port.jvp(q, x, lhs=(order == 1))
+    vj, _ = port.vjp(q, x, lhs=(order == 1))
+    assert np.abs(BJ.apply(jac, W, x) - jv).max() < 1e-14 * np.abs(jv).max()
+    assert np.abs(BJ.apply(jac, W, x, trans=True) - vj).max() < 1e-14 * np.abs(vj).max()
+    # the partners carry a first-order share of the product on these grids
+    assert np.abs(BJ.apply(jac, None, x) - jv).max() > 1e-3 * np.abs(jv).max()
+    A = BJ.to_sparse(jac, W)
+    assert np.abs(A @ x.ravel() - jv.ravel()).max() < 1e-14 * np.abs(jv).max()
+
+
+@pytest.mark.parametrize("turbulence,flux,order", VARIANTS)
+def test_wake_layout_reproduces_oracle_products(port_built, tmp_path, turbulence, flux, order):
+    c, port = naca(tmp_path, turbulence, flux)
+    products_match(c, port, C.perturbed_state(c, 11), order)
+
+
+@pytest.mark.parametrize("ni", [3, 4, 8])
+@pytest.mark.parametrize("turbulence,order", [("none", 2), ("sa", 2), ("none", 1)])
+def test_periodic_layout_reproduces_oracle_products(port_built, tmp_path, ni, turbulence, order):
+    c, port = channel(tmp_path, ni=ni, turbulence=turbulence)
+    products_match(c, port, C.perturbed_state(c, 12), order)
+
+
+def test_layout_refuses_what_it_cannot_hold(tmp_path):
+    c = C.naca0012_case(str(tmp_path), "n", ni=41, nj=9, tail=11, write_files=False)
+    c.boundaries[3].start = 0
+    with pytest.raises(ValueError):
+        BJ.partner_masks(c)
+    c.boundaries[3].start, c.boundaries[3].face = 1, "top"
+    with pytest.raises(ValueError):
+        BJ.partner_masks(c)
+    ch = C.channel_case(str(tmp_path), "ch", nj=11)
+    ch.boundaries[2].face = "bottom"
+    with pytest.raises(ValueError):
+        BJ.partner_masks(ch)
+    ch.boundaries[2].face, ch.boundaries[2].start = "left", 2
+    with pytest.raises(ValueError):
+        BJ.partner_masks(ch)
+    ch.boundaries[2].start = 0
+    ch.boundaries.append(C.Boundary("wake", "bottom", 1, 1))
+    with pytest.raises(ValueError):
+        BJ.partner_masks(ch)
+
+
+def test_newton_on_the_wake_coupled_jacobian_converges_superlinearly(port_built, tmp_path):
+    c, port = naca(tmp_path, ni=61, nj=17, tail=13)
+    q, hist = BJ.steady_newton(port, c, C.freestream_state(c))
+    assert hist[-1] < 1e-10, hist
+    # each of the last steps cuts the residual by more than the one before (the
+    # pseudo-time term 1/dt, CFL ~1e5 here, keeps it from being purely
+    # quadratic); an inexact Jacobian settles at a fixed factor
+    f = hist[-4:][1:] / hist[-4:][:-1]
+    assert (np.diff(f) < 0).all() and f[-1] < 0.05, hist[-4:]
+
+
+def test_newton_on_the_periodic_channel_converges(port_built, tmp_path):
+    c, port = channel(tmp_path, nj=21)
+    q, hist = BJ.steady_newton(port, c, C.freestream_state(c), cfl=10.0, growth=2.0, tol=1e-11)
+    assert hist[-1] < 1e-11, hist  # round-off floor ~2e-12 (1e-13 of the first residual)
+    # the steps above the round-off floor cut the residual by 1e-2 and more
+    f = hist[-4:][1:] / hist[-4:][:-1]
+    assert f[:2].max() < 0.02, hist[-4:]
+
+
+# ---------------------------------------------------------------------------
+# the device source on the host
+# ---------------------------------------------------------------------------
+GUARD = 64
+
+
+def guarded(n, fill=0.0, dtype=np.float64):
+    """Buffer of n elements inside NaN (or -7) guard bands; returns (whole, view)."""
+    g = np.full(n + 2 * GUARD, np.nan if dtype == np.float64 else -7, dtype=dtype)
+    g[GUARD:GUARD + n] = fill
+    return g, g[GUARD:GUARD + n]
+
+
+def guards_intact(g):
+    a, b = g[:GUARD], g[-GUARD:]
+    if g.dtype == np.float64:
+        return bool(np.isnan(a).all() and np.isnan(b).all())
+    return bool((a == -7).all() and (b == -7).all())
+
+
+@pytest.fixture(scope="module")
+def partner_host(tmp_path_factory):
+    here = os.path.dirname(os.path.abspath(__file__))
+    so = str(tmp_path_factory.mktemp("partner_host") / "libpartner_host.so")
+    subprocess.run(["g++", "-std=c++17", "-O1", "-Wall", "-Wno-unknown-pragmas", "-shared", "-fPIC", "-o", so,
+                    os.path.join(here, "partner_kernels_host.cpp")], check=True)
+    lib = ctypes.CDLL(so)
+    P = ctypes.c_void_p
+    I = ctypes.c_int
+    lib.ph_masks.argtypes = [I, I, P, I, P, P, P, P]
+    lib.ph_seed.argtypes = [I, I, I, I, P, I, I, P]
+    lib.ph_extract.argtypes = [I, I, I, I, P, I, I, P, P, P]
+    lib.ph_apply.argtypes = [I, I, I, I, I, P, P, P, ctypes.c_double]
+    return lib
+
+
+def host_masks(lib, c):
+    from structured_gb300 import abi
+    s, keep = abi.make_case_struct(c)
+    nic, njc = c.ni - 1, c.nj - 1
+    bufs = [guarded(nic, 0, np.int32), guarded(njc, 0, np.int32), guarded(njc, 0, np.int32)]
+    on = np.full(3, -1, dtype=np.int32)
+    rc = lib.ph_masks(nic, njc, ctypes.cast(s.bcs, ctypes.c_void_p), s.nbc, bufs[0][1].ctypes.data,
+                      bufs[1][1].ctypes.data, bufs[2][1].ctypes.data, on.ctypes.data)
+    assert all(guards_intact(g) for g, _ in bufs)
+    return rc, [m.astype(bool) for _, m in bufs], [bool(v) for v in on]
+
+
+def test_host_build_of_masks_agrees(partner_host, tmp_path):
+    cases = []
+    c = C.naca0012_case(str(tmp_path), "n", ni=41, nj=9, tail=11, write_files=False)
+    cases.append(c)
+    cases.append(C.channel_case(str(tmp_path), "ch", nj=11))
+    for c in cases:
+        rc, m, on = host_masks(partner_host, c)
+        masks, on_ref = BJ.partner_masks(c)
+        assert rc == 0 and on == on_ref
+        for f in range(3):
+            assert np.array_equal(m[f], masks[f])
+    c = C.naca0012_case(str(tmp_path), "n", ni=41, nj=9, tail=11, write_files=False)
+    c.boundaries[3].start = 0
+    assert host_masks(partner_host, c)[0] == -6
+    c.boundaries[3].start, c.boundaries[3].face = 1, "top"
+    assert host_masks(partner_host, c)[0] == -6
+    c.boundaries[3].type = "freestream"
+    rc, m, on = host_masks(partner_host, c)
+    assert rc == 0 and on == [False, False, False]
+    ch = C.channel_case(str(tmp_path), "ch", nj=11)
+    ch.boundaries[2].face = "top"
+    assert host_masks(partner_host, ch)[0] == -6
+    ch.boundaries[2].face, ch.boundaries[2].end = "left", 5
+    assert host_masks(partner_host, ch)[0] == -6
+    ch.boundaries[2].end = -1
+    ch.boundaries.append(C.Boundary("wake", "bottom", 1, 1))
+    assert host_masks(partner_host, ch)[0] == -6
+
+
+@pytest.mark.parametrize("which,turbulence,order", [("naca", "none", 2), ("naca", "sa", 1),
+                                                     ("channel2", "none", 2), ("channel5", "sa", 2)])
+def test_host_build_of_partner_pass_matches_restatement(port_built, partner_host, tmp_path, which, turbulence,
+                                                        order):
+    """The device source's seeds, extraction and products (run on the host over
+    the oracle's JVPs) equal the numpy layout and touch nothing outside their
+    buffers."""
+    if which == "naca":
+        c, port = naca(tmp_path, turbulence)
+    else:
+        c, port = channel(tmp_path, ni=3 if which == "channel2" else 6, turbulence=turbulence)
+    q = C.perturbed_state(c, 13)
+    nic, njc, nq = q.shape
+    rc, m, on = host_masks(partner_host, c)
+    assert rc == 0
+    ref = BJ.assemble_partners(port, q, *BJ.partner_masks(c), order)
+    zero = np.zeros((nic, njc, len(BJ.OFFSETS), nq, nq))
+    rng = np.random.default_rng(5)
+    for f in range(3):
+        if not on[f]:
+            continue
+        n = BJ.fam_len(f, nic, njc)
+        mask = np.ascontiguousarray(m[f].astype(np.int32))
+        gW, W = guarded(n * 4 * nq * nq)
+        for k in range(3):
+            for comp in range(nq):
+                gv, v = guarded(q.size, 0.0)
+                partner_host.ph_seed(nq, f, nic, njc, mask.ctypes.data, k, comp, v.ctypes.data)
+                assert guards_intact(gv)
+                seed = np.ascontiguousarray(v.reshape(q.shape))
+                full = port.jvp(q, seed, lhs=(order == 1))
+                port.freeze_nonlocal(True)
+                frozen = port.jvp(q, seed, lhs=(order == 1))
+                port.freeze_nonlocal(False)
+                gf, jf = guarded(q.size)
+                jf[:] = full.ravel()
+                gz, jz = guarded(q.size)
+                jz[:] = frozen.ravel()
+                partner_host.ph_extract(nq, f, nic, njc, mask.ctypes.data, k, comp, jf.ctypes.data, jz.ctypes.data,
+                                        W.ctypes.data)
+                assert guards_intact(gf) and guards_intact(gz) and guards_intact(gW)
+        assert np.array_equal(W.reshape(ref[f].shape), ref[f])
+        only = [None, None, None]
+        only[f] = ref[f]
+        for trans in (0, 1):
+            gx, x = guarded(q.size)
+            x[:] = rng.standard_normal(q.size)
+            gy, y = guarded(q.size)
+            y0 = rng.standard_normal(q.size)
+            y[:] = y0
+            partner_host.ph_apply(nq, trans, f, nic, njc, W.ctypes.data, x.ctypes.data, y.ctypes.data, -1.5)
+            assert guards_intact(gx) and guards_intact(gy) and guards_intact(gW)
+            want = y0 - 1.5 * BJ.apply(zero, only, x.reshape(q.shape), trans=bool(trans)).ravel()
+            assert np.abs(y - want).max() < 1e-14 * np.abs(want).max()
