@@ -682,8 +682,8 @@ int partner_setup(st_ctx* x) {
         x->pfam_on[f] = on[f] != 0;
         if (!on[f]) continue;
         const size_t len = (size_t)fam_len(f, nic, njc);
-        int rc = alloc_s(&x->pmask_d[f], len);
-        if (rc == ST_OK) rc = alloc_s(&x->wpart[f], len * NWS * x->nq * x->nq);
+        int rc = x->pmask_d[f] ? ST_OK : alloc_s(&x->pmask_d[f], len);
+        if (rc == ST_OK && !x->wpart[f]) rc = alloc_s(&x->wpart[f], len * NWS * x->nq * x->nq);
         if (rc) return rc;
         ST_CUDA(cudaMemcpyAsync(x->pmask_d[f], m[f].data(), len * sizeof(int), cudaMemcpyHostToDevice, x->stream));
         x->has_partners = true;
