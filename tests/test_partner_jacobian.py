@@ -314,3 +314,24 @@ def test_host_build_of_partner_pass_matches_restatement(port_built, partner_host
             assert guards_intact(gx) and guards_intact(gy) and guards_intact(gW)
             want = y0 - 1.5 * BJ.apply(zero, only, x.reshape(q.shape), trans=bool(trans)).ravel()
             assert np.abs(y - want).max() < 1e-14 * np.abs(want).max()
+
+
+def test_newton_on_the_channel_example_gives_poiseuille(port_built, tmp_path):
+    """The reference's implicit channel example (examples/laminar/channel/
+    implicit.inp: 3 x 101, h = 0.1, mu = 1e-2, dp/dx = -0.02592, periodic in x,
+    isothermal walls) by Newton through the periodic partner blocks: the
+    velocity has the Poiseuille shape (-dp/dx) / (2 mu) y (h - y) up to a
+    uniform offset (1 % of u_max on this grid, from the discretisation of the
+    walls), and v = 0."""
+    from oracle.port import PortCase
+    c = C.channel_case(str(tmp_path), "ch", nj=101)
+    xv, yv = C.load_grid(c)
+    q, hist = BJ.steady_newton(PortCase(c, xv, yv), c, C.freestream_state(c), cfl=10.0, growth=2.0, tol=3e-10)
+    assert hist[-1] < 3e-10, hist[-3:]  # round-off floor ~1.2e-10
+    u = q[:, :, 1] / q[:, :, 0]
+    yc = 0.25 * (yv[:-1, :-1] + yv[1:, :-1] + yv[:-1, 1:] + yv[1:, 1:])
+    exact = (-c.dpdx) / (2.0 * c.mu_inf) * yc * (0.1 - yc)
+    d = u - exact
+    assert d.max() - d.min() < 1e-5 * exact.max()
+    assert 0.0 < d.mean() < 0.02 * exact.max()
+    assert np.abs(q[:, :, 2] / q[:, :, 0]).max() < 1e-12 * exact.max()
