@@ -116,9 +116,12 @@ def test_periodic_channel_newton_matches_oracle_steady_state(gpu_lib, port_built
     q0 = C.freestream_state(c)
     eq = EulerEquation(c, xv, yv)
     eq.set_state(q0)
-    # the residual's round-off floor here is ~1e-11 (1e-12 of the first one)
+    # the residual's round-off floor here is ~1e-11 (1e-12 of the first one).  Two
+    # cells across, half of the i-coupling is periodic and outside the ILU, so
+    # GMRES stops at its iteration cap at high CFL; Newton still converges (a CPU
+    # emulation with ILU(0) and the cap at 400 reaches 1e-10 in 17 steps)
     ok, hist = Solver(eq, max_steps=100, cfl=10.0, cfl_ramp=0, cfl_growth=2.0, max_rel_drho=0.2, tolerance=1e-10,
-                      krylov_m=80, krylov_maxit=400, krylov_rtol=1e-8).solve()
+                      krylov_m=150, krylov_maxit=900, krylov_rtol=1e-8).solve()
     assert ok, hist[-3:]
     q_ref, h_ref = BJ.steady_newton(PortCase(c, xv, yv), c, q0, cfl=10.0, growth=2.0, tol=3e-11)
     assert h_ref[-1] < 3e-11
