@@ -48,7 +48,10 @@ struct st_ctx {
     std::vector<int> pmask[3];
     int* pmask_d[3] = {nullptr, nullptr, nullptr};
     double* wpart[3] = {nullptr, nullptr, nullptr};
-    bool partners_checked = false, has_partners = false;
+    // first-order partner blocks for the preconditioner when some partners lie
+    // in the ILU(0) pattern (pfold) and the operator is second order
+    double* wpart1[3] = {nullptr, nullptr, nullptr};
+    bool partners_checked = false, has_partners = false, pfold = false;
     bool pfam_on[3] = {false, false, false};
     // learned SA correction: BF16 weights, FP32 biases + normalisation, FP32
     // master parameters with Adam moments, training partials

@@ -118,6 +118,47 @@ __global__ void k_partner_extract(int f, int nic, int njc, const int* __restrict
     }
 }
 
+// Index of offset (di, dj) in the 13-point block row of the Jacobian
+// ((0,0), (-1,0), (1,0), (0,-1), (0,1), (-2,0), (2,0), (0,-2), (0,2),
+// (-1,-1), (-1,1), (1,-1), (1,1)); -1 outside it.
+__host__ __device__ inline int off13(int di, int dj) {
+    if (di == 0) return dj == 0 ? 0 : dj == -1 ? 3 : dj == 1 ? 4 : dj == -2 ? 7 : dj == 2 ? 8 : -1;
+    if (dj == 0) return di == -1 ? 1 : di == 1 ? 2 : di == -2 ? 5 : di == 2 ? 6 : -1;
+    if (di == -1) return dj == -1 ? 9 : dj == 1 ? 10 : -1;
+    if (di == 1) return dj == -1 ? 11 : dj == 1 ? 12 : -1;
+    return -1;
+}
+
+// Block-row offset of the partner of slot t at line position p when its
+// source lies in the row's 3x3 neighbourhood (the ILU(0) pattern), else -1.
+// Periodic boundaries two cells across put every partner there.
+__host__ __device__ inline int fold_offset(int f, int p, int t, int nic, int njc) {
+    const int b = p - wslot_d(t);
+    const size_t row = fam_row(f, p, t, nic, njc), src = fam_src(f, b, nic, njc);
+    const int di = (int)(src / njc) - (int)(row / njc), dj = (int)(src % njc) - (int)(row % njc);
+    return (di >= -1 && di <= 1 && dj >= -1 && dj <= 1) ? off13(di, dj) : -1;
+}
+
+// jac[row][o] += W[p][t] for the partners inside the ILU(0) pattern, so that
+// the preconditioner sees them; one thread per line position (its rows are
+// distinct from every other position's).  jac: [ncell][13][NQ][NQ].
+template <int NQ>
+__global__ void k_partner_fold(int f, int nic, int njc, const double* __restrict__ W, double* __restrict__ jac) {
+    const int len = fam_len(f, nic, njc);
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < len; p += gridDim.x * blockDim.x) {
+        for (int slot = 0; slot < NWS; slot++) {
+            const int b = p - wslot_d(slot);
+            if (b < 0 || b >= len) continue;
+            const int o = fold_offset(f, p, slot, nic, njc);
+            if (o < 0) continue;
+            double* dst = jac + (fam_row(f, p, slot, nic, njc) * 13 + o) * NQ * NQ;
+            const double* w = W + ((size_t)p * NWS + slot) * NQ * NQ;
+#pragma unroll
+            for (int e = 0; e < NQ * NQ; e++) dst[e] += w[e];
+        }
+    }
+}
+
 // acc += b x (TRANS: b^T x) for one nq x nq block
 template <int NQ, bool TRANS>
 __device__ inline void block_mv(const double* __restrict__ b, const double* __restrict__ x, double* acc) {

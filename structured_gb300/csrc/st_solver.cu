@@ -687,23 +687,33 @@ int partner_setup(st_ctx* x) {
         if (rc) return rc;
         ST_CUDA(cudaMemcpyAsync(x->pmask_d[f], m[f].data(), len * sizeof(int), cudaMemcpyHostToDevice, x->stream));
         x->has_partners = true;
+        for (int pp = 0; pp < (int)len; pp++)
+            for (int t = 0; t < NWS; t++) {
+                const int b = pp - wslot_d(t);
+                if (b >= 0 && b < (int)len && m[f][b] && fold_offset(f, pp, t, nic, njc) >= 0) x->pfold = true;
+            }
+    }
+    for (int f = 0; f < NFAM && x->pfold; f++) {
+        if (!on[f] || x->wpart1[f]) continue;
+        int rc = alloc_s(&x->wpart1[f], (size_t)fam_len(f, nic, njc) * NWS * x->nq * x->nq);
+        if (rc) return rc;
     }
     ST_CUDA(cudaStreamSynchronize(x->stream));
     x->partners_checked = true;
     return ST_OK;
 }
 
-// Partner blocks of the order-`order` residual into x->wpart[f]: per family,
+// Partner blocks of the order-`order` residual into out[f]: per family,
 // residue k and component, a full and a frozen JVP of the same seed (x->kz ->
 // x->kw, x->kr; both free during assembly).
-int assemble_partners(st_ctx* x, int order) {
+int assemble_partners(st_ctx* x, int order, double* const* out) {
     const int nq = x->nq, nic = x->c.ni - 1, njc = x->c.nj - 1;
     cudaStream_t s = x->stream;
     for (int f = 0; f < NFAM; f++) {
         if (!x->pfam_on[f]) continue;
         const int len = fam_len(f, nic, njc);
         const unsigned gl = grid_for((size_t)len), gw = grid_for((size_t)len * NWS);
-        ST_CUDA(cudaMemsetAsync(x->wpart[f], 0, (size_t)len * NWS * nq * nq * 8, s));
+        ST_CUDA(cudaMemsetAsync(out[f], 0, (size_t)len * NWS * nq * nq * 8, s));
         for (int k = 0; k < 3; k++) {
             bool seeded = false;
             for (int b = k; b < len; b += 3) seeded |= x->pmask[f][b] != 0;
@@ -716,13 +726,26 @@ int assemble_partners(st_ctx* x, int order) {
                 if (rc == ST_OK) rc = stx::run_jvp(x, x->kz, nullptr, x->kr, order, 1);
                 if (rc) return rc;
                 if (nq == 5)
-                    k_partner_extract<5><<<gw, 256, 0, s>>>(f, nic, njc, x->pmask_d[f], k, comp, x->kw, x->kr, x->wpart[f]);
+                    k_partner_extract<5><<<gw, 256, 0, s>>>(f, nic, njc, x->pmask_d[f], k, comp, x->kw, x->kr, out[f]);
                 else
-                    k_partner_extract<4><<<gw, 256, 0, s>>>(f, nic, njc, x->pmask_d[f], k, comp, x->kw, x->kr, x->wpart[f]);
+                    k_partner_extract<4><<<gw, 256, 0, s>>>(f, nic, njc, x->pmask_d[f], k, comp, x->kw, x->kr, out[f]);
             }
         }
     }
     ST_LAUNCH_CHECK("partner assembly");
+    return ST_OK;
+}
+
+// jac[row][o] += W for the partner blocks inside the ILU(0) pattern
+int fold_partners(st_ctx* x, double* const* W, double* jac) {
+    const int nic = x->c.ni - 1, njc = x->c.nj - 1;
+    for (int f = 0; f < NFAM; f++) {
+        if (!x->pfam_on[f]) continue;
+        const unsigned gl = grid_for((size_t)fam_len(f, nic, njc));
+        if (x->nq == 5) k_partner_fold<5><<<gl, 256, 0, x->stream>>>(f, nic, njc, W[f], jac);
+        else k_partner_fold<4><<<gl, 256, 0, x->stream>>>(f, nic, njc, W[f], jac);
+    }
+    ST_LAUNCH_CHECK("partner fold");
     return ST_OK;
 }
 
@@ -754,23 +777,33 @@ int assemble(st_ctx* x, int order) {
     int rc = partner_setup(x);
     if (rc == ST_OK) rc = ensure_solver(x, 1);
     if (rc == ST_OK) rc = assemble_into(x, order, x->jac);
-    if (rc == ST_OK && x->has_partners) rc = assemble_partners(x, order);
+    if (rc == ST_OK && x->has_partners) rc = assemble_partners(x, order, x->wpart);
     return rc;
 }
 
 // Operator Jacobian (order `order`) and, for the preconditioner, the
 // first-order Jacobian (reusing the operator when it is first order).  The
-// preconditioner keeps the regular blocks only: the partner blocks lie
-// outside the ILU(0) pattern.
+// preconditioner's ILU(0) pattern is the 3x3 neighbourhood: partner blocks
+// whose source lies in it (periodic boundaries two cells across) are folded
+// into the preconditioner's copy of the blocks, the others left out.
 int assemble_pair(st_ctx* x, int order) {
     int rc = assemble(x, order);
     if (rc) return rc;
-    if (order == 1) {
+    if (order == 1 && !x->pfold) {
         x->jac1_is_jac = true;
         return ST_OK;
     }
     x->jac1_is_jac = false;
-    return assemble_into(x, 1, x->jac1);
+    if (order == 1) {  // the operator's blocks plus its own (first-order) partners
+        ST_CUDA(cudaMemcpyAsync(x->jac1, x->jac, x->ncell * NOFF * x->nq * x->nq * 8, cudaMemcpyDeviceToDevice,
+                                x->stream));
+        return fold_partners(x, x->wpart, x->jac1);
+    }
+    rc = assemble_into(x, 1, x->jac1);
+    if (rc || !x->pfold) return rc;
+    rc = assemble_partners(x, 1, x->wpart1);
+    if (rc) return rc;
+    return fold_partners(x, x->wpart1, x->jac1);
 }
 
 struct LinOp {

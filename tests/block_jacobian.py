@@ -181,6 +181,19 @@ def apply(jac, W, x, trans: bool = False) -> np.ndarray:
     return y
 
 
+def fold(jac, W):
+    """The preconditioner's copy of the regular blocks with the partner blocks
+    whose source lies in the row's 3x3 neighbourhood (the ILU(0) pattern)
+    added, as st_solver.cu prepares it."""
+    out = jac.copy()
+    nic, njc = jac.shape[:2]
+    for (ri, rj), (si, sj), w in _partner_terms(W, nic, njc):
+        di, dj = si - ri, sj - rj
+        if abs(di) <= 1 and abs(dj) <= 1:
+            out[ri, rj, OFFSETS.index((di, dj))] += w
+    return out
+
+
 def to_sparse(jac, W):
     """The same operator as a scipy CSR matrix over (i*njc + j)*nq + k
     (duplicate entries are summed)."""

@@ -46,4 +46,11 @@ void ph_apply(int nq, int trans, int f, int nic, int njc, const double* W, const
     }
 }
 
+int ph_off13(int di, int dj) { return off13(di, dj); }
+
+void ph_fold(int nq, int f, int nic, int njc, const double* W, double* jac) {
+    if (nq == 5) k_partner_fold<5>(f, nic, njc, W, jac);
+    else k_partner_fold<4>(f, nic, njc, W, jac);
+}
+
 }  // extern "C"

@@ -216,6 +216,8 @@ def partner_host(tmp_path_factory):
     lib.ph_seed.argtypes = [I, I, I, I, P, I, I, P]
     lib.ph_extract.argtypes = [I, I, I, I, P, I, I, P, P, P]
     lib.ph_apply.argtypes = [I, I, I, I, I, P, P, P, ctypes.c_double]
+    lib.ph_off13.argtypes = [I, I]
+    lib.ph_fold.argtypes = [I, I, I, I, P, P]
     return lib
 
 
@@ -335,3 +337,36 @@ def test_newton_on_the_channel_example_gives_poiseuille(port_built, tmp_path):
     assert d.max() - d.min() < 1e-5 * exact.max()
     assert 0.0 < d.mean() < 0.02 * exact.max()
     assert np.abs(q[:, :, 2] / q[:, :, 0]).max() < 1e-12 * exact.max()
+
+
+def test_host_build_of_offset_index_matches_the_layout(partner_host):
+    for o, (di, dj) in enumerate(BJ.OFFSETS):
+        assert partner_host.ph_off13(di, dj) == o
+    assert partner_host.ph_off13(2, 1) == -1 and partner_host.ph_off13(-1, 2) == -1
+
+
+@pytest.mark.parametrize("which,turbulence", [("channel2", "none"), ("channel3", "sa"), ("naca", "none")])
+def test_host_build_of_fold_matches_restatement(port_built, partner_host, tmp_path, which, turbulence):
+    """Partner blocks inside the ILU(0) pattern are added to the
+    preconditioner's blocks, nothing outside the buffer changes.  Two cells
+    across every partner is inside; three across only the slots one cell in,
+    which are zero at first order; none for the wake cut of this grid."""
+    if which == "naca":
+        c, port = naca(tmp_path, turbulence)
+    else:
+        c, port = channel(tmp_path, ni=3 if which == "channel2" else 4, turbulence=turbulence)
+    q = C.perturbed_state(c, 17)
+    nic, njc, nq = q.shape
+    masks, on = BJ.partner_masks(c)
+    jac = BJ.assemble_regular(port, q, 1)
+    W = BJ.assemble_partners(port, q, masks, on, 1)
+    ref = BJ.fold(jac, W)
+    gj, flat = guarded(jac.size)
+    flat[:] = jac.ravel()
+    for f in range(3):
+        if on[f]:
+            partner_host.ph_fold(nq, f, nic, njc, np.ascontiguousarray(W[f]).ctypes.data, flat.ctypes.data)
+    assert guards_intact(gj)
+    assert np.array_equal(flat.reshape(jac.shape), ref)
+    changed = not np.array_equal(ref, jac)
+    assert changed == (which == "channel2")
