@@ -117,9 +117,9 @@ def test_periodic_channel_newton_matches_oracle_steady_state(gpu_lib, port_built
     eq = EulerEquation(c, xv, yv)
     eq.set_state(q0)
     # the residual's round-off floor here is ~1e-11 (1e-12 of the first one).  Two
-    # cells across, half of the i-coupling is periodic and outside the ILU, so
-    # GMRES stops at its iteration cap at high CFL; Newton still converges (a CPU
-    # emulation with ILU(0) and the cap at 400 reaches 1e-10 in 17 steps)
+    # cells across, half of the i-coupling is periodic; the preconditioner folds
+    # those partner blocks in (a CPU emulation of ILU(0) without them needs the
+    # full iteration cap at high CFL and still converges in 17 steps)
     ok, hist = Solver(eq, max_steps=100, cfl=10.0, cfl_ramp=0, cfl_growth=2.0, max_rel_drho=0.2, tolerance=1e-10,
                       krylov_m=150, krylov_maxit=900, krylov_rtol=1e-8).solve()
     assert ok, hist[-3:]
