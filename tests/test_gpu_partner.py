@@ -147,3 +147,28 @@ def test_refused_boundary_lists(gpu_lib, tmp_path):
     with pytest.raises(StructuredError) as e:
         eq.jacobian_assemble()
     assert e.value.code == -6
+
+
+def test_naca_example_size_matches_oracle_target(gpu_lib, tmp_path):
+    """The laminar NACA 0012 example's flow on the generated 281 x 151 C-grid
+    (the example's size, its wake cut and wall) solved implicitly on the GPU:
+    Cl and Cd equal the oracle's Newton state's (tests/golden/
+    make_naca_target.py, Cl/Cd through the reference's wall gradients)."""
+    import json
+    import os
+    from structured_gb300 import io
+    from structured_gb300.solver import EulerEquation, Solver
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "naca0012_281x151_target.json")
+    target = json.load(open(path))["forces"]
+    c = C.naca0012_case(str(tmp_path), "naca", ni=281, nj=151, tail=41)
+    c.lhs_order = 2
+    eq = EulerEquation(c, *C.load_grid(c))
+    eq.set_state(C.freestream_state(c))
+    # the oracle's Newton reaches 8.5e-10 in 30 steps; the round-off floor is ~4e-10
+    ok, hist = Solver(eq, max_steps=150, cfl=1.0, cfl_ramp=0, cfl_growth=1.5, max_rel_drho=0.2, tolerance=2e-9,
+                      krylov_m=150, krylov_maxit=900, krylov_rtol=1e-6).solve()
+    assert ok, hist[-3:]
+    f = io.write_outputs(eq, str(tmp_path / "naca"))
+    size = abs(target["cl"]) + abs(target["cd"])
+    for k in ("cl", "cd", "cl_pressure", "cd_pressure", "cl_viscous", "cd_viscous"):
+        assert abs(f[k] - target[k]) <= 1e-6 * size, (k, f[k], target[k])
