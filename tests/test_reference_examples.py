@@ -71,3 +71,27 @@ def test_partner_layout_on_the_naca_example_grid(port_built):
     assert np.abs(A @ x.ravel() - jv.ravel()).max() < 1e-13 * np.abs(jv).max()
     # (transposed products against the oracle's VJP: tests/test_partner_jacobian.py,
     # on grids where the oracle's dense VJP path is affordable)
+
+
+def test_surface_file_on_the_naca_example_matches_the_reference(ref_available, tmp_path):
+    """IOManager::write_surface on the C-grid example (wall faces tail-1 ..
+    ni-tail-1 of the j = 0 row, src/utils/io.cpp:182-255): this package's
+    writer, given the reference's wall gradients, writes the same bytes."""
+    if not ref_available:
+        pytest.skip("reference sources not mounted")
+    from oracle.refcase import RefCase
+    from structured_gb300 import io
+    d, c, (xv, yv) = example("naca0012", "config.inp")
+    text = open(os.path.join(d, "config.inp")).read()
+    text = text.replace('filename = "grid.unf2"', 'filename = "%s"' % c.grid_path)
+    text = text.replace('label = "implicit"', 'label = "%s"' % str(tmp_path / "ref"))
+    inp = tmp_path / "config.inp"
+    inp.write_text(text)
+    ref = RefCase(str(inp))
+    q = C.perturbed_state(c, 21)
+    ref.residual(q)  # fills the reference's face gradients of this state
+    grad = np.ascontiguousarray(ref.eta_gradients()[:, 0, :])
+    ref.write_outputs(q)
+    forces = io.write_surface(str(tmp_path / "ours.surface"), c, xv, yv, q, grad)
+    assert (tmp_path / "ours.surface").read_bytes() == (tmp_path / "ref.surface").read_bytes()
+    assert all(np.isfinite(v) for v in forces.values())
