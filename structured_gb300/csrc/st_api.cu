@@ -557,9 +557,10 @@ int st_destroy(st_ctx* x) {
                       x->cf, x->wall_dx_d, x->Pbar, x->srec, x->arec_i, x->arec_j, x->psi_tmp,
                       x->outq_tmp, x->outb_tmp, x->tape, x->jac, x->jac1, x->kv, x->kzb, x->kz, x->kw, x->kr, x->kh, x->kpart, x->dq, x->qsave,
                       x->qtmp, x->wpart[0], x->wpart[1], x->wpart[2], x->wpart1[0], x->wpart1[1], x->wpart1[2],
-                      x->wallg};
+                      x->wallg, x->strip_jac_d, x->strip_dt_d, x->strip_inv_d, x->strip_res_d};
     for (double* b : bufs) if (b) cudaFree(b);
     for (int* m : x->pmask_d) if (m) cudaFree(m);
+    if (x->strip_cells_d) cudaFree(x->strip_cells_d);
     st::dual* dbufs[] = {x->qd, x->Pd, x->limd, x->Fdi, x->Fdj, x->Gdi, x->Gdj, x->rhsd, x->betad};
     for (st::dual* b : dbufs) if (b) cudaFree(b);
     if (x->bcs_d) cudaFree(x->bcs_d);

@@ -52,6 +52,15 @@ struct st_ctx {
     // in the ILU(0) pattern (pfold) and the operator is second order
     double* wpart1[3] = {nullptr, nullptr, nullptr};
     bool partners_checked = false, has_partners = false, pfold = false;
+    // wake strip preconditioner level (st_partner.cuh): strip cells, their
+    // gathered blocks and time steps, the inverse of the strip block, a
+    // residual buffer; strip_W1 the first-order wake partners it uses
+    std::vector<int> strip_cells;
+    int strip_ns = 0;
+    int* strip_cells_d = nullptr;
+    double *strip_jac_d = nullptr, *strip_dt_d = nullptr, *strip_inv_d = nullptr, *strip_res_d = nullptr;
+    const double* strip_W1 = nullptr;
+    bool strip_ready = false;
     bool pfam_on[3] = {false, false, false};
     // learned SA correction: BF16 weights, FP32 biases + normalisation, FP32
     // master parameters with Adam moments, training partials

@@ -213,4 +213,164 @@ __global__ void k_partner_apply(int f, int nic, int njc, const double* __restric
     }
 }
 
+// ---------------------------------------------------------------------------
+// Wake strip: a second preconditioner level for the wake cut, whose partner
+// blocks lie outside the ILU(0) pattern.  The strip is rows 0 and 1 of every
+// column within one of a wake ghost column (it holds each wake partner's row
+// and source).  After the ILU sweep z = M^-1 v, the correction
+//   z_S += A_SS^-1 (v - P z)_S,   P = psd D + sj (J1 + W1),
+// with A_SS the strip's block of P (dense, inverted on the host once per
+// factorisation), solves the strip's coupling exactly.
+// ---------------------------------------------------------------------------
+__host__ __device__ inline int off_di(int o) {
+    return o == 1 || o == 9 || o == 10 ? -1 : o == 2 || o == 11 || o == 12 ? 1 : o == 5 ? -2 : o == 6 ? 2 : 0;
+}
+__host__ __device__ inline int off_dj(int o) {
+    return o == 3 || o == 9 || o == 11 ? -1 : o == 4 || o == 10 || o == 12 ? 1 : o == 7 ? -2 : o == 8 ? 2 : 0;
+}
+
+// strip cells in increasing cell order into cells[] (room for 2 nic); returns the count
+inline int strip_cells(int nic, int njc, const int* mask_wake, int* cells) {
+    int n = 0;
+    for (int i = 0; i < nic; i++) {
+        const bool on = mask_wake[i] || (i > 0 && mask_wake[i - 1]) || (i + 1 < nic && mask_wake[i + 1]);
+        if (!on) continue;
+        for (int j = 0; j < 2 && j < njc; j++) cells[n++] = i * njc + j;
+    }
+    return n;
+}
+
+// index of cell c in the sorted strip, -1 if absent
+__host__ __device__ inline int strip_find(int ns, const int* cells, long c) {
+    int lo = 0, hi = ns - 1;
+    while (lo <= hi) {
+        const int mid = (lo + hi) / 2;
+        if (cells[mid] == c) return mid;
+        if (cells[mid] < c) lo = mid + 1;
+        else hi = mid - 1;
+    }
+    return -1;
+}
+
+// Dense strip block A (n = ns nq, row-major) of psd D + sj (J1 + W1): jac_s the
+// strip cells' 13 regular blocks [ns][13][nq][nq], dt_s their time steps
+// [ns][nq] (NULL: no D term), W1 the first-order wake partners [nic][4][nq][nq].
+inline void strip_matrix(int nic, int njc, int nq, int ns, const int* cells, const double* jac_s, const double* dt_s,
+                         const double* W1, double psd, double sj, double* A) {
+    const int n = ns * nq;
+    for (long e = 0; e < (long)n * n; e++) A[e] = 0.0;
+    auto add = [&](int a, int b, const double* blk, double f) {
+        for (int k = 0; k < nq; k++)
+            for (int l = 0; l < nq; l++) A[(long)(a * nq + k) * n + b * nq + l] += f * blk[k * nq + l];
+    };
+    for (int a = 0; a < ns; a++) {
+        const int ri = cells[a] / njc, rj = cells[a] % njc;
+        if (dt_s)
+            for (int k = 0; k < nq; k++) A[(long)(a * nq + k) * n + a * nq + k] += psd / dt_s[a * nq + k];
+        for (int o = 0; o < 13; o++) {
+            const int ci = ri + off_di(o), cj = rj + off_dj(o);
+            if (ci < 0 || ci >= nic || cj < 0 || cj >= njc) continue;
+            const int b = strip_find(ns, cells, (long)ci * njc + cj);
+            if (b >= 0) add(a, b, jac_s + ((size_t)a * 13 + o) * nq * nq, sj);
+        }
+        for (int t = 0; t < NWS; t++) {
+            if (wslot_j(t) != rj) continue;
+            const int g = ri - wslot_d(t);
+            if (g < 0 || g >= nic) continue;
+            const int b = strip_find(ns, cells, (long)fam_src(FAM_WAKE, g, nic, njc));
+            if (b >= 0) add(a, b, W1 + ((size_t)ri * NWS + t) * nq * nq, sj);
+        }
+    }
+}
+
+// inv = A^-1 by Gauss-Jordan elimination with partial pivoting (A is
+// overwritten); returns 0 if a pivot vanishes
+inline int dense_invert(int n, double* A, double* inv) {
+    for (long e = 0; e < (long)n * n; e++) inv[e] = 0.0;
+    for (int i = 0; i < n; i++) inv[(long)i * n + i] = 1.0;
+    for (int c = 0; c < n; c++) {
+        int p = c;
+        double best = A[(long)c * n + c] < 0 ? -A[(long)c * n + c] : A[(long)c * n + c];
+        for (int r = c + 1; r < n; r++) {
+            const double v = A[(long)r * n + c] < 0 ? -A[(long)r * n + c] : A[(long)r * n + c];
+            if (v > best) { best = v; p = r; }
+        }
+        if (!(best > 0.0)) return 0;
+        if (p != c)
+            for (int l = 0; l < n; l++) {
+                double t = A[(long)c * n + l]; A[(long)c * n + l] = A[(long)p * n + l]; A[(long)p * n + l] = t;
+                t = inv[(long)c * n + l]; inv[(long)c * n + l] = inv[(long)p * n + l]; inv[(long)p * n + l] = t;
+            }
+        const double d = 1.0 / A[(long)c * n + c];
+        for (int l = 0; l < n; l++) { A[(long)c * n + l] *= d; inv[(long)c * n + l] *= d; }
+        for (int r = 0; r < n; r++) {
+            if (r == c) continue;
+            const double f = A[(long)r * n + c];
+            if (f == 0.0) continue;
+            for (int l = 0; l < n; l++) {
+                A[(long)r * n + l] -= f * A[(long)c * n + l];
+                inv[(long)r * n + l] -= f * inv[(long)c * n + l];
+            }
+        }
+    }
+    return 1;
+}
+
+// the strip cells' regular blocks and time steps, compacted for the host
+template <int NQ>
+__global__ void k_strip_gather(int ns, const int* __restrict__ cells, const double* __restrict__ jac,
+                               const double* __restrict__ dt, double* __restrict__ jac_s, double* __restrict__ dt_s) {
+    const size_t per = 13 * NQ * NQ, n = (size_t)ns * per;
+    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+        const size_t a = e / per, w = e % per;
+        jac_s[e] = jac[(size_t)cells[a] * per + w];
+        if (dt && w < NQ) dt_s[a * NQ + w] = dt[(size_t)cells[a] * NQ + w];
+    }
+}
+
+// res = (v - P z) on the strip, one thread per strip cell
+template <int NQ>
+__global__ void k_strip_residual(int nic, int njc, int ns, const int* __restrict__ cells,
+                                 const double* __restrict__ jac, const double* __restrict__ W1,
+                                 const double* __restrict__ dt, double psd, double sj, const double* __restrict__ v,
+                                 const double* __restrict__ z, double* __restrict__ res) {
+    for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < ns; a += gridDim.x * blockDim.x) {
+        const size_t r = (size_t)cells[a];
+        const int ri = (int)(r / njc), rj = (int)(r % njc);
+        double acc[NQ];
+#pragma unroll
+        for (int k = 0; k < NQ; k++) acc[k] = 0.0;
+        for (int o = 0; o < 13; o++) {
+            const int ci = ri + off_di(o), cj = rj + off_dj(o);
+            if (ci < 0 || ci >= nic || cj < 0 || cj >= njc) continue;
+            block_mv<NQ, false>(jac + (r * 13 + o) * NQ * NQ, z + ((size_t)ci * njc + cj) * NQ, acc);
+        }
+        for (int t = 0; t < NWS; t++) {
+            if (wslot_j(t) != rj) continue;
+            const int g = ri - wslot_d(t);
+            if (g < 0 || g >= nic) continue;
+            block_mv<NQ, false>(W1 + ((size_t)ri * NWS + t) * NQ * NQ, z + fam_src(FAM_WAKE, g, nic, njc) * NQ, acc);
+        }
+#pragma unroll
+        for (int k = 0; k < NQ; k++) {
+            double pz = sj * acc[k];
+            if (dt) pz += psd * z[r * NQ + k] / dt[r * NQ + k];
+            res[(size_t)a * NQ + k] = v[r * NQ + k] - pz;
+        }
+    }
+}
+
+// z_S += Ainv res, one thread per strip unknown (rows of Ainv are distinct)
+template <int NQ>
+__global__ void k_strip_update(int ns, const int* __restrict__ cells, const double* __restrict__ Ainv,
+                               const double* __restrict__ res, double* __restrict__ z) {
+    const int n = ns * NQ;
+    for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < n; m += gridDim.x * blockDim.x) {
+        double s = 0.0;
+        const double* row = Ainv + (size_t)m * n;
+        for (int l = 0; l < n; l++) s += row[l] * res[l];
+        z[(size_t)cells[m / NQ] * NQ + m % NQ] += s;
+    }
+}
+
 }  // namespace st

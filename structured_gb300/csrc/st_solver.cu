@@ -25,6 +25,7 @@ using stx::grid_for;
 namespace {
 
 constexpr int NOFF = 13;
+constexpr int STRIP_MAX = 1024;  // largest wake strip (unknowns) given a dense inverse
 // stencil offsets (di, dj) of the block Jacobian row; 0 is the diagonal block
 __constant__ int c_di[NOFF] = {0, -1, 1, 0, 0, -2, 2, 0, 0, -1, -1, 1, 1};
 __constant__ int c_dj[NOFF] = {0, 0, 0, -1, 1, 0, 0, -2, 2, -1, 1, -1, 1};
@@ -693,7 +694,26 @@ int partner_setup(st_ctx* x) {
                 if (b >= 0 && b < (int)len && m[f][b] && fold_offset(f, pp, t, nic, njc) >= 0) x->pfold = true;
             }
     }
-    for (int f = 0; f < NFAM && x->pfold; f++) {
+    // the wake strip level (not where a fold already puts wake partners into
+    // the ILU, and only while its dense block stays small)
+    if (on[FAM_WAKE] && !x->pfold) {
+        std::vector<int> cells(2 * (size_t)nic);
+        const int ns = strip_cells(nic, njc, m[FAM_WAKE].data(), cells.data());
+        if (ns > 0 && ns * x->nq <= STRIP_MAX) {
+            cells.resize(ns);
+            x->strip_cells = cells;
+            x->strip_ns = ns;
+            const size_t n = (size_t)ns * x->nq;
+            int rc = x->strip_cells_d ? ST_OK : alloc_s(&x->strip_cells_d, (size_t)ns);
+            if (rc == ST_OK && !x->strip_jac_d) rc = alloc_s(&x->strip_jac_d, (size_t)ns * NOFF * x->nq * x->nq);
+            if (rc == ST_OK && !x->strip_dt_d) rc = alloc_s(&x->strip_dt_d, n);
+            if (rc == ST_OK && !x->strip_inv_d) rc = alloc_s(&x->strip_inv_d, n * n);
+            if (rc == ST_OK && !x->strip_res_d) rc = alloc_s(&x->strip_res_d, n);
+            if (rc) return rc;
+            ST_CUDA(cudaMemcpyAsync(x->strip_cells_d, cells.data(), ns * sizeof(int), cudaMemcpyHostToDevice, x->stream));
+        }
+    }
+    for (int f = 0; f < NFAM && (x->pfold || x->strip_ns > 0); f++) {
         if (!on[f] || x->wpart1[f]) continue;
         int rc = alloc_s(&x->wpart1[f], (size_t)fam_len(f, nic, njc) * NWS * x->nq * x->nq);
         if (rc) return rc;
@@ -789,21 +809,26 @@ int assemble(st_ctx* x, int order) {
 int assemble_pair(st_ctx* x, int order) {
     int rc = assemble(x, order);
     if (rc) return rc;
-    if (order == 1 && !x->pfold) {
-        x->jac1_is_jac = true;
-        return ST_OK;
-    }
-    x->jac1_is_jac = false;
-    if (order == 1) {  // the operator's blocks plus its own (first-order) partners
+    x->strip_W1 = nullptr;
+    if (order == 1) {
+        if (x->strip_ns > 0) x->strip_W1 = x->wpart[FAM_WAKE];
+        if (!x->pfold) {
+            x->jac1_is_jac = true;
+            return ST_OK;
+        }
+        // the operator's blocks plus its own (first-order) partners
+        x->jac1_is_jac = false;
         ST_CUDA(cudaMemcpyAsync(x->jac1, x->jac, x->ncell * NOFF * x->nq * x->nq * 8, cudaMemcpyDeviceToDevice,
                                 x->stream));
         return fold_partners(x, x->wpart, x->jac1);
     }
+    x->jac1_is_jac = false;
     rc = assemble_into(x, 1, x->jac1);
-    if (rc || !x->pfold) return rc;
+    if (rc || !(x->pfold || x->strip_ns > 0)) return rc;
     rc = assemble_partners(x, 1, x->wpart1);
     if (rc) return rc;
-    return fold_partners(x, x->wpart1, x->jac1);
+    if (x->strip_ns > 0) x->strip_W1 = x->wpart1[FAM_WAKE];
+    return x->pfold ? fold_partners(x, x->wpart1, x->jac1) : ST_OK;
 }
 
 struct LinOp {
@@ -849,8 +874,36 @@ int check_err(st_ctx* x, const char* what) {
 }
 
 // one cluster of ILU_CL CTAs walks the levels
+// The wake strip level for a forward solve: gather the strip's blocks, build
+// and invert its dense block on the host, upload the inverse.  A singular or
+// non-finite block leaves the plain ILU(0).
+int strip_factor(st_ctx* x, const LinOp& op, const double* j1) {
+    const int nic = x->c.ni - 1, njc = x->c.nj - 1, nq = x->nq, ns = x->strip_ns, n = ns * nq;
+    cudaStream_t s = x->stream;
+    const size_t nb = (size_t)ns * NOFF * nq * nq;
+    if (nq == 5) k_strip_gather<5><<<grid_for(nb), 256, 0, s>>>(ns, x->strip_cells_d, j1, op.pdt, x->strip_jac_d, x->strip_dt_d);
+    else k_strip_gather<4><<<grid_for(nb), 256, 0, s>>>(ns, x->strip_cells_d, j1, op.pdt, x->strip_jac_d, x->strip_dt_d);
+    ST_LAUNCH_CHECK("strip gather");
+    std::vector<double> jac_s(nb), dt_s((size_t)n), w1((size_t)nic * NWS * nq * nq);
+    ST_CUDA(cudaMemcpyAsync(jac_s.data(), x->strip_jac_d, nb * 8, cudaMemcpyDeviceToHost, s));
+    if (op.pdt) ST_CUDA(cudaMemcpyAsync(dt_s.data(), x->strip_dt_d, (size_t)n * 8, cudaMemcpyDeviceToHost, s));
+    ST_CUDA(cudaMemcpyAsync(w1.data(), x->strip_W1, w1.size() * 8, cudaMemcpyDeviceToHost, s));
+    ST_CUDA(cudaStreamSynchronize(s));
+    std::vector<double> A((size_t)n * n), inv((size_t)n * n);
+    strip_matrix(nic, njc, nq, ns, x->strip_cells.data(), jac_s.data(), op.pdt ? dt_s.data() : nullptr, w1.data(),
+                 op.psd, op.sj, A.data());
+    if (!dense_invert(n, A.data(), inv.data())) return ST_OK;
+    for (double v : inv)
+        if (!std::isfinite(v)) return ST_OK;
+    ST_CUDA(cudaMemcpyAsync(x->strip_inv_d, inv.data(), inv.size() * 8, cudaMemcpyHostToDevice, s));
+    ST_CUDA(cudaStreamSynchronize(s));
+    x->strip_ready = true;
+    return ST_OK;
+}
+
 int factor_M(st_ctx* x, const LinOp& op) {
     const int nic = x->c.ni - 1, njc = x->c.nj - 1;
+    x->strip_ready = false;
     ST_CUDA(cudaMemsetAsync(x->err_d, 0, sizeof(int), x->stream));
     const double* j1 = x->jac1_is_jac ? x->jac : x->jac1;
     if (x->nq == 5)
@@ -858,7 +911,9 @@ int factor_M(st_ctx* x, const LinOp& op) {
     else
         k_ilu_factor<4><<<ILU_CL, ILU_THREADS, 0, x->stream>>>(nic, njc, j1, op.pdt, op.psd, op.sj, x->lfac, x->err_d);
     ST_LAUNCH_CHECK("ILU factorisation");
-    return check_err(x, "ILU factorisation");
+    int rc = check_err(x, "ILU factorisation");
+    if (rc == ST_OK && !op.trans && x->strip_ns > 0 && x->strip_W1) rc = strip_factor(x, op, j1);
+    return rc;
 }
 
 int apply_M(st_ctx* x, const LinOp& op, const double* in, double* out) {
@@ -881,6 +936,22 @@ int apply_M(st_ctx* x, const LinOp& op, const double* in, double* out) {
         else k_ilu_solve<4, false><<<ILU_CL, ILU_THREADS, 0, s>>>(nic, njc, x->lfac, in, out);
     }
     ST_LAUNCH_CHECK("ILU solve");
+    if (!op.trans && x->strip_ready) {
+        const double* j1 = x->jac1_is_jac ? x->jac : x->jac1;
+        const int ns = x->strip_ns;
+        if (x->nq == 5) {
+            k_strip_residual<5><<<grid_for((size_t)ns), 256, 0, s>>>(nic, njc, ns, x->strip_cells_d, j1, x->strip_W1,
+                                                                    op.pdt, op.psd, op.sj, in, out, x->strip_res_d);
+            k_strip_update<5><<<grid_for((size_t)ns * 5), 256, 0, s>>>(ns, x->strip_cells_d, x->strip_inv_d,
+                                                                      x->strip_res_d, out);
+        } else {
+            k_strip_residual<4><<<grid_for((size_t)ns), 256, 0, s>>>(nic, njc, ns, x->strip_cells_d, j1, x->strip_W1,
+                                                                    op.pdt, op.psd, op.sj, in, out, x->strip_res_d);
+            k_strip_update<4><<<grid_for((size_t)ns * 4), 256, 0, s>>>(ns, x->strip_cells_d, x->strip_inv_d,
+                                                                      x->strip_res_d, out);
+        }
+        ST_LAUNCH_CHECK("wake strip correction");
+    }
     return ST_OK;
 }
 

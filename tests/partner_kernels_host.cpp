@@ -53,4 +53,32 @@ void ph_fold(int nq, int f, int nic, int njc, const double* W, double* jac) {
     else k_partner_fold<4>(f, nic, njc, W, jac);
 }
 
+int ph_strip_cells(int nic, int njc, const int* mask_wake, int* cells) {
+    return strip_cells(nic, njc, mask_wake, cells);
+}
+
+void ph_strip_matrix(int nic, int njc, int nq, int ns, const int* cells, const double* jac_s, const double* dt_s,
+                     const double* W1, double psd, double sj, double* A) {
+    strip_matrix(nic, njc, nq, ns, cells, jac_s, dt_s, W1, psd, sj, A);
+}
+
+int ph_dense_invert(int n, double* A, double* inv) { return dense_invert(n, A, inv); }
+
+void ph_strip_gather(int nq, int ns, const int* cells, const double* jac, const double* dt, double* jac_s,
+                     double* dt_s) {
+    if (nq == 5) k_strip_gather<5>(ns, cells, jac, dt, jac_s, dt_s);
+    else k_strip_gather<4>(ns, cells, jac, dt, jac_s, dt_s);
+}
+
+void ph_strip_residual(int nq, int nic, int njc, int ns, const int* cells, const double* jac, const double* W1,
+                       const double* dt, double psd, double sj, const double* v, const double* z, double* res) {
+    if (nq == 5) k_strip_residual<5>(nic, njc, ns, cells, jac, W1, dt, psd, sj, v, z, res);
+    else k_strip_residual<4>(nic, njc, ns, cells, jac, W1, dt, psd, sj, v, z, res);
+}
+
+void ph_strip_update(int nq, int ns, const int* cells, const double* Ainv, const double* res, double* z) {
+    if (nq == 5) k_strip_update<5>(ns, cells, Ainv, res, z);
+    else k_strip_update<4>(ns, cells, Ainv, res, z);
+}
+
 }  // extern "C"

@@ -218,6 +218,13 @@ def partner_host(tmp_path_factory):
     lib.ph_apply.argtypes = [I, I, I, I, I, P, P, P, ctypes.c_double]
     lib.ph_off13.argtypes = [I, I]
     lib.ph_fold.argtypes = [I, I, I, I, P, P]
+    D = ctypes.c_double
+    lib.ph_strip_cells.argtypes = [I, I, P, P]
+    lib.ph_strip_matrix.argtypes = [I, I, I, I, P, P, P, P, D, D, P]
+    lib.ph_dense_invert.argtypes = [I, P, P]
+    lib.ph_strip_gather.argtypes = [I, I, P, P, P, P, P]
+    lib.ph_strip_residual.argtypes = [I, I, I, I, P, P, P, P, D, D, P, P, P]
+    lib.ph_strip_update.argtypes = [I, I, P, P, P, P]
     return lib
 
 
@@ -370,3 +377,74 @@ def test_host_build_of_fold_matches_restatement(port_built, partner_host, tmp_pa
     assert np.array_equal(flat.reshape(jac.shape), ref)
     changed = not np.array_equal(ref, jac)
     assert changed == (which == "channel2")
+
+
+@pytest.mark.parametrize("turbulence", ["none", "sa"])
+def test_host_build_of_wake_strip_level_matches_restatement(port_built, partner_host, tmp_path, turbulence):
+    """The wake strip level (rows 0-1 of the columns next to the cut): its
+    cells, the dense strip block of P = psd D + sj (J1 + W1) and its inverse,
+    and the correction z_S += A_SS^-1 (v - P z)_S, from the device source run on
+    the host, against numpy on the oracle's blocks."""
+    import scipy.sparse as sp
+    c, port = naca(tmp_path, turbulence)
+    q = C.perturbed_state(c, 19)
+    nic, njc, nq = q.shape
+    masks, on = BJ.partner_masks(c)
+    jac1 = BJ.assemble_regular(port, q, 1)
+    W1 = BJ.assemble_partners(port, q, masks, on, 1)
+    mask = np.ascontiguousarray(masks[0].astype(np.int32))
+    gcells, cells_buf = guarded(2 * nic, 0, np.int32)
+    ns = partner_host.ph_strip_cells(nic, njc, mask.ctypes.data, cells_buf.ctypes.data)
+    assert guards_intact(gcells)
+    cells = np.ascontiguousarray(cells_buf[:ns])
+    want = sorted(i * njc + j for i in range(nic) for j in (0, 1)
+                  if masks[0][max(i - 1, 0):i + 2].any())
+    assert cells.tolist() == want
+    dt = port.dt(q, 30.0)
+    # gather
+    gjs, jac_s = guarded(ns * 13 * nq * nq)
+    gds, dt_s = guarded(ns * nq)
+    jflat = np.ascontiguousarray(jac1.ravel())
+    dflat = np.ascontiguousarray(dt.ravel())
+    partner_host.ph_strip_gather(nq, ns, cells.ctypes.data, jflat.ctypes.data, dflat.ctypes.data,
+                                 jac_s.ctypes.data, dt_s.ctypes.data)
+    assert guards_intact(gjs) and guards_intact(gds)
+    cell_ij = [(int(cl) // njc, int(cl) % njc) for cl in cells]
+    assert np.array_equal(jac_s.reshape(ns, 13, nq, nq), np.stack([jac1[i, j] for i, j in cell_ij]))
+    assert np.array_equal(dt_s.reshape(ns, nq), np.stack([dt[i, j] for i, j in cell_ij]))
+    # strip block of P
+    psd, sj = 1.0, -1.0
+    P = (sp.diags(psd / dt.ravel()) + sj * BJ.to_sparse(jac1, W1)).tocsr()
+    idx = np.array([int(cl) * nq + k for cl in cells for k in range(nq)])
+    A_ref = P[idx][:, idx].toarray()
+    n = ns * nq
+    gA, A = guarded(n * n)
+    w1 = np.ascontiguousarray(W1[0])
+    partner_host.ph_strip_matrix(nic, njc, nq, ns, cells.ctypes.data, jac_s.ctypes.data, dt_s.ctypes.data,
+                                 w1.ctypes.data, psd, sj, A.ctypes.data)
+    assert guards_intact(gA)
+    assert np.abs(A.reshape(n, n) - A_ref).max() <= 1e-14 * np.abs(A_ref).max()
+    gI, inv = guarded(n * n)
+    assert partner_host.ph_dense_invert(n, A.ctypes.data, inv.ctypes.data) == 1
+    assert guards_intact(gI)
+    I_err = np.abs(inv.reshape(n, n) @ A_ref - np.eye(n)).max()
+    assert I_err < 1e-9, I_err
+    # correction
+    rng = np.random.default_rng(8)
+    v = np.ascontiguousarray(rng.standard_normal(q.size))
+    gz, z = guarded(q.size)
+    z0 = rng.standard_normal(q.size)
+    z[:] = z0
+    gr, res = guarded(n)
+    partner_host.ph_strip_residual(nq, nic, njc, ns, cells.ctypes.data, jflat.ctypes.data, w1.ctypes.data,
+                                   dflat.ctypes.data, psd, sj, v.ctypes.data, z.ctypes.data, res.ctypes.data)
+    assert guards_intact(gr) and guards_intact(gz)
+    res_ref = (v - P @ z0)[idx]
+    assert np.abs(res - res_ref).max() <= 1e-13 * np.abs(res_ref).max()
+    partner_host.ph_strip_update(nq, ns, cells.ctypes.data, inv.ctypes.data, res.ctypes.data, z.ctypes.data)
+    assert guards_intact(gz)
+    z_ref = z0.copy()
+    z_ref[idx] += inv.reshape(n, n) @ res_ref
+    assert np.abs(z - z_ref).max() <= 1e-12 * np.abs(z_ref).max()
+    # after the correction the strip rows of P z equal v
+    assert np.abs((P @ z)[idx] - v[idx]).max() <= 1e-9 * np.abs(v).max()
