@@ -219,6 +219,45 @@ def to_sparse(jac, W):
     return sp.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))), shape=(n, n))
 
 
+def block_ilu0(M, nic: int, njc: int, nq: int):
+    """Block ILU(0) of a sparse matrix over the 3x3 neighbourhood in natural
+    cell order (the preconditioner st_solver.cu factors, here in FP64);
+    returns the solve v -> (LU)^-1 v."""
+    M = M.tocsr()
+    n = nic * njc
+    nbrs = []
+    for c in range(n):
+        i, j = divmod(c, njc)
+        nbrs.append(sorted(ii * njc + jj for ii in (i - 1, i, i + 1) for jj in (j - 1, j, j + 1)
+                           if 0 <= ii < nic and 0 <= jj < njc))
+    blk = {(r, c): M[r * nq:(r + 1) * nq, c * nq:(c + 1) * nq].toarray() for r in range(n) for c in nbrs[r]}
+    inv = [None] * n
+    for r in range(n):
+        for k in nbrs[r]:
+            if k >= r:
+                break
+            blk[(r, k)] = blk[(r, k)] @ inv[k]
+            for j in nbrs[k]:
+                if j > k and (r, j) in blk:
+                    blk[(r, j)] = blk[(r, j)] - blk[(r, k)] @ blk[(k, j)]
+        inv[r] = np.linalg.inv(blk[(r, r)])
+
+    def solve(v):
+        y = np.asarray(v, dtype=float).reshape(n, nq).copy()
+        for r in range(n):
+            for k in nbrs[r]:
+                if k >= r:
+                    break
+                y[r] -= blk[(r, k)] @ y[k]
+        for r in range(n - 1, -1, -1):
+            for j in nbrs[r]:
+                if j > r:
+                    y[r] -= blk[(r, j)] @ y[j]
+            y[r] = inv[r] @ y[r]
+        return y.ravel()
+    return solve
+
+
 def steady_newton(port, c, q, cfl=1.0, growth=1.5, cfl_max=1e8, max_rel_drho=0.2, tol=1e-10, max_steps=80):
     """Steady state of the oracle's residual by pseudo-time Newton: each step
     solves (I/dt - J) dq = R, the implicit solver's system, exactly (sparse LU
