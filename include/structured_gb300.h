@@ -232,6 +232,18 @@ int st_adjoint_solve_device(st_ctx* ctx, const double* b_dev, double* psi_dev, d
 int st_tangent_solve_device(st_ctx* ctx, const double* b_dev, double* dq_dev, double cfl_prec, int krylov_m,
                             int maxit, double rtol, st_solve_stats* stats);
 
+/* State of the implicit solve's preconditioner after the last factorisation
+ * (st_solve, st_linear_solve_device): strip_unknowns = unknowns of the wake
+ * strip level (0: no wake cut, partner blocks folded into the ILU(0) pattern
+ * instead, or more than 1024 unknowns, in which case only the block ILU(0)
+ * runs); strip_active = 1 if the last forward factorisation built the strip's
+ * inverse (0 after a transposed one, or when its dense block was singular);
+ * strip_factorisations counts strip builds; strip_host_ms is the host time of
+ * the last one (gather, dense inverse, upload).  Any pointer may be NULL.
+ * No counterpart in the reference (its sparse LU needs no preconditioner). */
+int st_precond_info(st_ctx* ctx, int* strip_unknowns, int* strip_active, int* strip_factorisations,
+                    double* strip_host_ms);
+
 /* Kernel launches one st_residual_device / st_vjp_device call makes. */
 int st_launch_counts(st_ctx* ctx, int lhs, int* residual, int* vjp);
 
@@ -243,8 +255,10 @@ int st_launch_counts(st_ctx* ctx, int lhs, int* residual, int* vjp);
  * the device for its own pool, or a loop that cannot afford the device-wide
  * synchronisation of cudaMalloc/cudaFree): its partial sums live in a fixed
  * 64 KiB device array inside the library, held by every device that loads it
- * until the process exits.  Limit: nq <= 8.  The first call on each device
- * looks up that array's address (cudaGetSymbolAddress); make it outside any
+ * until the process exits.  Limit: nq <= 8.  Every call looks up that
+ * array's address on the current device (cudaGetSymbolAddress, which
+ * allocates nothing), so the address survives a device reset; the first call
+ * on a device loads the library's device code there, so make it outside any
  * stream capture.  All calls share the array: calls that overlap on the GPU
  * race. */
 int st_norms_noalloc(const double* rhs_dev, long long ncell, int nq, double* out_dev, void* stream);
@@ -269,11 +283,23 @@ int st_mlp_enable(st_ctx* ctx, int on);
  * raw; targets [n]); loss_host (optional) receives one loss per step. */
 int st_mlp_train(st_ctx* ctx, const float* feat_dev, const float* target_dev, long n, int steps, int batch, float lr,
                  unsigned long long seed, float* loss_host);
+/* Gradient of the training loss of one batch, without an update: the batch
+ * st_mlp_train draws at its step `step` (0-based count of steps since
+ * st_mlp_init) with this seed, the same forward and backward kernels and the
+ * same fixed-order reduction, in the FP32 master layout
+ * (grad_host[st_mlp_param_count()]); loss_host (optional) the batch loss. */
+int st_mlp_grad(st_ctx* ctx, const float* feat_dev, const float* target_dev, long n, int batch,
+                unsigned long long seed, int step, float* grad_host, float* loss_host);
 int st_sa_features(st_ctx* ctx, float* feat_dev);           /* raw features of the state, [ncell][4] */
 int st_mlp_beta(st_ctx* ctx, double* beta_dev);             /* network beta of the state, [ncell] */
 
 /* Diagnostics: dense FP64 FMA throughput of this device (TFLOP/s). */
 int st_probe_fp64(st_ctx* ctx, double* tflops);
+/* Diagnostics: the kernels' Newton-Raphson reciprocal and square roots on a
+ * device array x_dev[n] of positive normal doubles; out_dev[n][5] receives
+ * 1/x, 1/sqrt(x), sqrt(x), and the (sqrt(x), 1/sqrt(x)) pair of the combined
+ * routine, for tests against correctly rounded values.  Synchronises. */
+int st_probe_nr_math(const double* x_dev, long long n, double* out_dev);
 /* Runs one pipeline on the context state (which = 0: residual; 1: adjoint VJP
  * with psi = the context's last residual; 2: residual + VJP in one sweep) with a CUDA event after every
  * launch: ms[k] is the device time of launch k, names a comma-separated list

@@ -38,34 +38,34 @@ __device__ inline double sgn(double x) { return x < 0.0 ? -1.0 : 1.0; }
 struct RoeTape {
     double rlft, ulft, vlft, plft, rrht, urht, vrht, prht, r1, r2, aj;
     double rlfti, rulft, rvlft, uvl, elft, hlft, rrhti, rurht, rvrht, uvr, erht, hrht;
-    double rat, rati, rav, uav, vav, hav, uv, cav, aq1, aq2, aq3, aq4, uu, c2, c2i, auu, aupc, aumc;
+    double rat, irat, rati, rav, uav, vav, hav, uv, cav, icav, aq1, aq2, aq3, aq4, uu, c2, c2i, auu, aupc, aumc;
     double uulft, uurht, rcav, aquu, c2ih, ruuav, t2, t3, b1, b2, b3, b4, b5, b6, b7, eplft, eprht;
     double f[4];
 };
 
 __device__ inline void roe_fwd(RoeTape& t) {
-    t.rlfti = 1.0 / t.rlft;
+    t.rlfti = nr_rcp(t.rlft);
     t.rulft = t.rlft * t.ulft; t.rvlft = t.rlft * t.vlft;
     t.uvl = 0.5 * (t.ulft * t.ulft + t.vlft * t.vlft);
     t.elft = t.plft * OGM1 + t.rlft * t.uvl;
     t.hlft = (t.elft + t.plft) * t.rlfti;
-    t.rrhti = 1.0 / t.rrht;
+    t.rrhti = nr_rcp(t.rrht);
     t.rurht = t.rrht * t.urht; t.rvrht = t.rrht * t.vrht;
     t.uvr = 0.5 * (t.urht * t.urht + t.vrht * t.vrht);
     t.erht = t.prht * OGM1 + t.rrht * t.uvr;
     t.hrht = (t.erht + t.prht) * t.rrhti;
-    t.rat = ::sqrt(t.rrht * t.rlfti);
-    t.rati = 1.0 / (t.rat + 1.0);
+    t.rat = nr_sqrt_inv(t.rrht * t.rlfti, &t.irat);
+    t.rati = nr_rcp(t.rat + 1.0);
     t.rav = t.rat * t.rlft;
     t.uav = (t.rat * t.urht + t.ulft) * t.rati;
     t.vav = (t.rat * t.vrht + t.vlft) * t.rati;
     t.hav = (t.rat * t.hrht + t.hlft) * t.rati;
     t.uv = 0.5 * (t.uav * t.uav + t.vav * t.vav);
-    t.cav = ::sqrt(GM1 * (t.hav - t.uv));
+    t.cav = nr_sqrt_inv(GM1 * (t.hav - t.uv), &t.icav);
     t.aq1 = t.rrht - t.rlft; t.aq2 = t.urht - t.ulft; t.aq3 = t.vrht - t.vlft; t.aq4 = t.prht - t.plft;
     t.uu = t.r1 * t.uav + t.r2 * t.vav;
     t.c2 = t.cav * t.cav;
-    t.c2i = 1.0 / t.c2;
+    t.c2i = t.icav * t.icav;
     t.auu = ::fabs(t.uu); t.aupc = ::fabs(t.uu + t.cav); t.aumc = ::fabs(t.uu - t.cav);
     t.uulft = t.r1 * t.ulft + t.r2 * t.vlft; t.uurht = t.r1 * t.urht + t.r2 * t.vrht;
     t.rcav = t.rav * t.cav;
@@ -146,7 +146,7 @@ __device__ inline void roe_rev(const RoeTape& t, const double* fb, double* bl, d
     uav_ += uu_ * r1; vav_ += uu_ * r2;
     rrht_ += aq1_; rlft_ -= aq1_; urht_ += aq2_; ulft_ -= aq2_; vrht_ += aq3_; vlft_ -= aq3_; prht_ += aq4_; plft_ -= aq4_;
     {
-        const double tmp = cav_ * GM1 * 0.5 / t.cav;
+        const double tmp = cav_ * GM1 * 0.5 * t.icav;
         hav_ += tmp;
         uav_ -= tmp * t.uav; vav_ -= tmp * t.vav;
     }
@@ -160,7 +160,7 @@ __device__ inline void roe_rev(const RoeTape& t, const double* fb, double* bl, d
     rat_ += -rati_ * t.rati * t.rati;
     double rlfti_ = 0, rrhti_ = 0;
     {
-        const double tmp = rat_ * 0.5 / t.rat;
+        const double tmp = rat_ * 0.5 * t.irat;
         rrht_ += tmp * t.rlfti; rlfti_ += tmp * rrht;
     }
     erht_ += hrht_ * t.rrhti; prht_ += hrht_ * t.rrhti; rrhti_ += hrht_ * (t.erht + t.prht);
@@ -184,12 +184,16 @@ __device__ inline void roe_rev(const RoeTape& t, const double* fb, double* bl, d
 }
 
 // Reverse of sa_source (same forward formulas); outputs adjoints of rho, nut,
-// mu, omega, |grad nut|^2 and beta for source adjoint sb.
+// mu, omega, |grad nut|^2 and beta for source adjoint sb.  Each quotient's
+// reciprocal is formed once (Newton-Raphson, st_common.cuh) and shared by the
+// forward and reverse sweeps; fw's sixth root is (g^6 + cw3^6)^(-1/6) = q, so
+// d fw / d g^6 needs q^6 = 1 / (g^6 + cw3^6) and no further division.
 __device__ inline double sa_source_adj(double rho, double nut, double mu, double d, double omega, double gnut2,
                                        double beta, double sb, double* rho_, double* nut_, double* mu_,
                                        double* omega_, double* gnut2_, double* beta_) {
+    const double id2 = nr_rcp(d * d);
     if (nut < 0.0) {  // SA-neg branch of sa_source
-        const double cp = SA_CB1 * (1.0 - SA_CT3), id2 = 1.0 / (d * d);
+        const double cp = SA_CB1 * (1.0 - SA_CT3);
         const double src = beta * cp * omega * nut + SA_CW1 * nut * nut * id2;
         *rho_ = sb * (src + (SA_CB2 / SA_SIGMA) * gnut2);
         *nut_ = sb * rho * (beta * cp * omega + 2.0 * SA_CW1 * nut * id2);
@@ -199,27 +203,29 @@ __device__ inline double sa_source_adj(double rho, double nut, double mu, double
         *beta_ = sb * rho * cp * omega * nut;
         return rho * src + (SA_CB2 / SA_SIGMA) * rho * gnut2;
     }
-    const double k2d2 = SA_KAPPA * SA_KAPPA * d * d;
-    const double chi = rho * nut / mu;
+    const double ik2d2 = id2 * (1.0 / (SA_KAPPA * SA_KAPPA));
+    const double imu = nr_rcp(mu);
+    const double chi = rho * nut * imu;
     const double chi3 = chi * chi * chi;
-    const double den = chi3 + SA_CV1_3;
-    const double fv1 = chi3 / den;
-    const double E = 1.0 + chi * fv1;
-    const double fv2 = 1.0 - chi / E;
-    const double sbar = nut * fv2 * (1.0 / k2d2);
+    const double iden = nr_rcp(chi3 + SA_CV1_3);
+    const double fv1 = chi3 * iden;
+    const double iE = nr_rcp(1.0 + chi * fv1);
+    const double fv2 = 1.0 - chi * iE;
+    const double sbar = nut * fv2 * ik2d2;
     const bool br1 = sbar >= -SA_CV2 * omega;
-    double stilde, N = 0, D = 1;
+    double stilde, N = 0.0, iD = 1.0;
     if (br1) {
         stilde = omega + sbar;
     } else {
         N = SA_CV2 * SA_CV2 * omega + SA_CV3 * sbar;
-        D = (SA_CV3 - 2.0 * SA_CV2) * omega - sbar;
-        stilde = omega + omega * N / D;
+        iD = nr_rcp((SA_CV3 - 2.0 * SA_CV2) * omega - sbar);
+        stilde = omega + omega * N * iD;
     }
-    double r;
+    double r, ist = 0.0;
     bool rfree = false;
     if (stilde > 0.0) {
-        r = nut / (stilde * k2d2);
+        ist = nr_rcp(stilde);
+        r = nut * ist * ik2d2;
         if (r < 10.0) rfree = true; else r = 10.0;
     } else {
         r = 10.0;
@@ -227,52 +233,53 @@ __device__ inline double sa_source_adj(double rho, double nut, double mu, double
     const double r2 = r * r;
     const double gg = r + SA_CW2 * (r2 * r2 * r2 - r);
     const double g2 = gg * gg;
-    const double g6 = g2 * g2 * g2;
-    const double z = (1.0 + SA_CW3_6) / (g6 + SA_CW3_6);
-    const double h = ::cbrt(::sqrt(z));
+    const double q = nr_inv_root6(g2 * g2 * g2 + SA_CW3_6);
+    const double h = SA_C6 * q;
     const double fw = gg * h;
     const double prod = beta * SA_CB1 * stilde * nut;
-    const double dest = SA_CW1 * fw * (nut * nut) / (d * d);
+    const double dest = SA_CW1 * fw * (nut * nut) * id2;
     // reverse
     double rhob = sb * (prod - dest + (SA_CB2 / SA_SIGMA) * gnut2);
     const double prod_ = sb * rho, dest_ = -sb * rho;
     *gnut2_ = sb * rho * (SA_CB2 / SA_SIGMA);
-    double fw_ = dest_ * SA_CW1 * nut * nut / (d * d);
-    double nutb = dest_ * SA_CW1 * fw * 2.0 * nut / (d * d);
+    double fw_ = dest_ * SA_CW1 * nut * nut * id2;
+    double nutb = dest_ * SA_CW1 * fw * 2.0 * nut * id2;
     *beta_ = prod_ * SA_CB1 * stilde * nut;
     double stilde_ = prod_ * beta * SA_CB1 * nut;
     nutb += prod_ * beta * SA_CB1 * stilde;
     double gg_ = fw_ * h;
     const double h_ = fw_ * gg;
-    const double z_ = h_ * h / (6.0 * z);
-    const double g6_ = -z_ * z / (g6 + SA_CW3_6);
+    // h = C6 w^(-1/6), w = g^6 + cw3^6: dh/dw = -(1/6) h / w = -(1/6) h q^6
+    const double q2 = q * q;
+    const double g6_ = h_ * h * (q2 * q2 * q2) * (-1.0 / 6.0);
     const double g2_ = g6_ * 3.0 * g2 * g2;
     gg_ += g2_ * 2.0 * gg;
     const double r_ = gg_ * (1.0 + SA_CW2 * (6.0 * r2 * r2 * r - 1.0));
     if (rfree) {
-        nutb += r_ / (stilde * k2d2);
-        stilde_ += -r_ * r / stilde;
+        nutb += r_ * ist * ik2d2;
+        stilde_ += -r_ * r * ist;
     }
     double omegab = 0.0, sbar_ = 0.0;
     if (br1) {
         omegab += stilde_;
         sbar_ += stilde_;
     } else {
-        omegab += stilde_ * (1.0 + N / D);
-        const double N_ = stilde_ * omega / D;
-        const double D_ = -stilde_ * omega * N / (D * D);
+        omegab += stilde_ * (1.0 + N * iD);
+        const double N_ = stilde_ * omega * iD;
+        const double D_ = -stilde_ * omega * N * (iD * iD);
         omegab += N_ * SA_CV2 * SA_CV2 + D_ * (SA_CV3 - 2.0 * SA_CV2);
         sbar_ += N_ * SA_CV3 - D_;
     }
-    nutb += sbar_ * fv2 / k2d2;
-    const double fv2_ = sbar_ * nut / k2d2;
-    double chi_ = -fv2_ / E + fv2_ * chi * fv1 / (E * E);
-    const double fv1_ = fv2_ * chi * chi / (E * E);
-    const double chi3_ = fv1_ * SA_CV1_3 / (den * den);
+    nutb += sbar_ * fv2 * ik2d2;
+    const double fv2_ = sbar_ * nut * ik2d2;
+    const double iE2 = iE * iE;
+    double chi_ = -fv2_ * iE + fv2_ * chi * fv1 * iE2;
+    const double fv1_ = fv2_ * chi * chi * iE2;
+    const double chi3_ = fv1_ * SA_CV1_3 * (iden * iden);
     chi_ += chi3_ * 3.0 * chi * chi;
-    rhob += chi_ * nut / mu;
-    nutb += chi_ * rho / mu;
-    *mu_ = -chi_ * chi / mu;
+    rhob += chi_ * nut * imu;
+    nutb += chi_ * rho * imu;
+    *mu_ = -chi_ * chi * imu;
     *rho_ = rhob;
     *nut_ = nutb;
     *omega_ = omegab;
@@ -416,9 +423,9 @@ __global__ void __launch_bounds__(256, 2) k_face_fused(DevCase c, const double* 
             if (NQ == 5) {
                 mutb = 0.375 * (pL[P_MUT] + pR[P_MUT]) + 0.0625 * (pPa[P_MUT] + pPb[P_MUT] + pMa[P_MUT] + pMb[P_MUT]);
                 mu = mub + mutb;
-                k = c.cp * (mub * (1.0 / c.pr) + mutb * (1.0 / PR_TURB));
+                k = mub * c.cp_pr + mutb * c.cp_prt;
             } else {
-                k = mub * (c.cp / c.pr);
+                k = mub * c.cp_pr;
             }
             const double nx = gm[G_NX], ny = gm[G_NY];
             const double div = dudx + dvdy;
@@ -446,8 +453,8 @@ __global__ void __launch_bounds__(256, 2) k_face_fused(DevCase c, const double* 
             double dudy_ = txy_ * mu, dvdx_ = txy_ * mu;
             dudx_ += div_; dvdy_ += div_;
             double mub_ = mu_, mutb_ = 0.0;
-            if (NQ == 5) { mutb_ = mu_ + k_ * c.cp / PR_TURB; mub_ += k_ * c.cp / c.pr; }
-            else mub_ += k_ * (c.cp / c.pr);
+            if (NQ == 5) { mutb_ = mu_ + k_ * c.cp_prt; mub_ += k_ * c.cp_pr; }
+            else mub_ += k_ * c.cp_pr;
             o[A_DTDX] = dTdx_; o[A_DTDY] = dTdy_;
             o[A_UB] = ub_; o[A_VB] = vb_;
             if (NQ == 5) {
@@ -694,7 +701,7 @@ __global__ void __launch_bounds__(1024) k_bc_adj(DevCase c, const double* __rest
                                                  double* __restrict__ Pbar) {
     const int nic = c.nic, njc = c.njc;
     const int nr = ring_size(c);
-    const double iR = 1.0 / c.R;
+    const double iR = c.iR;
     if (c.viscous) {
         for (int r = threadIdx.x; r < nr; r += blockDim.x) {
             int ip, jp;
@@ -845,24 +852,24 @@ __global__ void __launch_bounds__(256) k_prim_adj(DevCase c, const double* __res
         const double* Q = q + idx * NQ;
         const double* p = P + pidx(c, i + 1, j + 1);
         const double* b = Pbar + pidx(c, i + 1, j + 1);
-        const double rho = Q[0], ri = 1.0 / rho, u = p[P_U], v = p[P_V];
+        const double rho = Q[0], ri = nr_rcp(rho), u = p[P_U], v = p[P_V];
         double rhob = b[P_RHO], ub = b[P_U], vb = b[P_V], pb = b[P_P], Tb = b[P_T], nutb = b[P_NUT], mub = b[P_MU];
         if (c.viscous) {
             const double mu = p[P_MU];
             if (NQ == 5 && p[P_NUT] >= 0.0) {  // mu_t = 0 for nut < 0
                 const double s = rho * p[P_NUT];
-                const double chi = s / mu, chi3 = chi * chi * chi, den = chi3 + SA_CV1_3;
-                const double f = chi3 / den, fp = 3.0 * chi * chi * SA_CV1_3 / (den * den);
+                const double chi = s * nr_rcp(mu), chi3 = chi * chi * chi, iden = nr_rcp(chi3 + SA_CV1_3);
+                const double f = chi3 * iden, fp = 3.0 * chi * chi * SA_CV1_3 * (iden * iden);
                 const double ds = f + chi * fp;
                 rhob += b[P_MUT] * ds * p[P_NUT];
                 nutb += b[P_MUT] * ds * rho;
                 mub += b[P_MUT] * (-chi * chi * fp);
             }
-            const double T = p[P_T];
-            const double dmu = c.law == 1 ? mu * (1.5 / T - 1.0 / (T + c.suth_S)) : (2.0 / 3.0) * mu / T;
+            const double iT = nr_rcp(p[P_T]);
+            const double dmu = c.law == 1 ? mu * (1.5 * iT - nr_rcp(p[P_T] + c.suth_S)) : (2.0 / 3.0) * mu * iT;
             Tb += mub * dmu;
         }
-        const double iR = 1.0 / c.R;
+        const double iR = c.iR;
         pb += Tb * ri * iR;
         double rib = Tb * p[P_P] * iR;
         double Qb[5] = {0, 0, 0, 0, 0};

@@ -292,6 +292,21 @@ __global__ void k_dfma_probe(double* out, int iters, double a, double b) {
     if (s == 12345.678) out[0] = s;
 }
 
+// Newton-Raphson reciprocal and square roots of st_common.cuh on a device
+// array: out[i][0..4] = nr_rcp, nr_rsqrt, nr_sqrt, nr_sqrt_inv (root, inverse)
+__global__ void k_nr_probe(const double* __restrict__ x, size_t n, double* __restrict__ out) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const double v = x[i];
+        double inv;
+        const double s = nr_sqrt_inv(v, &inv);
+        out[i * 5 + 0] = nr_rcp(v);
+        out[i * 5 + 1] = nr_rsqrt(v);
+        out[i * 5 + 2] = nr_sqrt(v);
+        out[i * 5 + 3] = s;
+        out[i * 5 + 4] = inv;
+    }
+}
+
 template <class T>
 int alloc(T** p, size_t n) {
     cudaError_t e = cudaMalloc((void**)p, std::max<size_t>(n, 1) * sizeof(T));
@@ -534,8 +549,12 @@ int st_create(const st_case* c, const double* xv, const double* yv, int device, 
     dc.R = c->p_inf / c->rho_inf / c->T_inf;  // src/model/fluid.cpp:12
     dc.cp = GAMMA * dc.R / (GAMMA - 1.0);
     dc.pr = c->pr_inf;
+    dc.cp_pr = dc.cp / dc.pr;
+    dc.cp_prt = dc.cp / PR_TURB;
+    dc.iR = 1.0 / dc.R;
     dc.rho_inf = c->rho_inf; dc.u_inf = c->u_inf; dc.v_inf = c->v_inf; dc.p_inf = c->p_inf;
     dc.T_inf = c->T_inf; dc.mu_inf = c->mu_inf; dc.nut_inf = c->nu_tilde_inf;
+    dc.iT_inf = 1.0 / dc.T_inf;
     dc.suth_S = 110.4 / 288.15 * c->T_inf;
     dc.eps_chi = std::pow(10.0 / nic, 3);  // src/model/reconstruction.cpp:59-60
     dc.eps_eta = std::pow(10.0 / njc, 3);
@@ -732,6 +751,14 @@ int st_probe_fp64(st_ctx* x, double* tflops) {
     cudaEventDestroy(e1);
     if (err != cudaSuccess) return stx::cuda_fail(err, "st_probe_fp64");
     *tflops = 2.0 * blocks * threads * (double)iters * 8 / (ms * 1e-3) / 1e12;
+    return ST_OK;
+}
+
+int st_probe_nr_math(const double* x_dev, long long n, double* out_dev) {
+    if (!x_dev || !out_dev || n < 1) return fail(ST_ERR_ARG, "st_probe_nr_math: bad argument");
+    k_nr_probe<<<grid_for((size_t)n), 256>>>(x_dev, (size_t)n, out_dev);
+    ST_LAUNCH_CHECK("st_probe_nr_math");
+    ST_CUDA(cudaDeviceSynchronize());
     return ST_OK;
 }
 

@@ -34,6 +34,7 @@ constexpr double SA_CW2 = 0.3, SA_CW3 = 2.0, SA_CV1 = 7.1, SA_CV2 = 0.7, SA_CV3 
 constexpr double SA_CW1 = SA_CB1 / (SA_KAPPA * SA_KAPPA) + (1.0 + SA_CB2) / SA_SIGMA;
 constexpr double SA_CV1_3 = SA_CV1 * SA_CV1 * SA_CV1;
 constexpr double SA_CW3_6 = SA_CW3 * SA_CW3 * SA_CW3 * SA_CW3 * SA_CW3 * SA_CW3;
+constexpr double SA_C6 = 2.005174745150421541;  // (1 + c_w3^6)^(1/6) = 65^(1/6)
 // negative-nu_tilde branch (SA-neg: Allmaras, Johnson & Spalart, ICCFD7-1902, 2012)
 constexpr double SA_CT3 = 1.2, SA_CN1 = 16.0;
 constexpr double PR_TURB = 0.9;
@@ -54,6 +55,8 @@ struct DevCase {
     int viscous, sa, law, nbc;
     int flux;              // ST_FLUX_ROE / ST_FLUX_AUSM
     double R, cp, pr, rho_inf, u_inf, v_inf, p_inf, T_inf, mu_inf, nut_inf;
+    double cp_pr, cp_prt;  // c_p / Pr and c_p / Pr_t (heat conductivity per unit viscosity)
+    double iR, iT_inf;     // 1 / R, 1 / T_inf
     double suth_S, eps_chi, eps_eta, dpdx, dpdy;
     const double* vol;     // [nic][njc]
     const double* ivol;    // [nic][njc] 1/vol
@@ -74,6 +77,67 @@ __host__ __device__ inline size_t pidx(const DevCase& c, int ip, int jp) {
 }
 
 // ---------------------------------------------------------------------------
+// Reciprocal and square roots by Newton-Raphson refinement of the hardware
+// approximations (PTX rcp.approx.ftz.f64 / rsqrt.approx.ftz.f64).  The FP64
+// pipe issues about two instructions per clock per SM on this part, and the
+// IEEE-rounded divide and square root take about ten of them each; a Newton
+// step squares the relative error, so two steps from the hardware seed reach
+// FP64 round-off (within a few ulp of the correctly rounded result; the GPU
+// tests bound the error against 1.0 / x and sqrt(x)).  Inputs: positive,
+// finite, normal numbers (densities, pressures, viscosities, sound speeds).
+//   nr_rcp:   r <- r + r (1 - x r), twice                      (4 DFMA)
+//   nr_rsqrt: y <- y + y (1/2 - (x/2) y^2), twice               (7)
+//   nr_sqrt:  one rsqrt step, s = x y, then s + (y/2)(x - s^2)  (8)
+//   nr_sqrt_inv: sqrt(x) and 1/sqrt(x) (two rsqrt steps, then the correction)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double nr_rcp(double x) {
+    double r;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+    double e = fma(-x, r, 1.0);
+    r = fma(r, e, r);
+    e = fma(-x, r, 1.0);
+    return fma(r, e, r);
+}
+__device__ __forceinline__ double rsqrt_seed(double x) {
+    double y;
+    asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+    return y;
+}
+__device__ __forceinline__ double nr_rsqrt(double x) {
+    double y = rsqrt_seed(x);
+    const double mh = -0.5 * x;
+    y = fma(y, fma(mh * y, y, 0.5), y);
+    return fma(y, fma(mh * y, y, 0.5), y);
+}
+__device__ __forceinline__ double nr_sqrt(double x) {
+    double y = rsqrt_seed(x);
+    y = fma(y, fma(-0.5 * x * y, y, 0.5), y);
+    const double s = x * y;
+    return fma(0.5 * y, fma(-s, s, x), s);
+}
+__device__ __forceinline__ double nr_sqrt_inv(double x, double* inv) {
+    const double y = nr_rsqrt(x);
+    const double s = x * y;
+    *inv = y;
+    return fma(0.5 * y, fma(-s, s, x), s);
+}
+
+// w^(-1/6) for positive w below FP32 overflow (3e38) by Newton's iteration on q^-6 - w = 0,
+// q <- q + (q/6)(1 - w q^6), twice from an FP32 seed w^(-1/6) by the fast
+// single-precision power (about 18 correct bits; each step roughly squares
+// the error, times 3.5).
+__device__ __forceinline__ double nr_inv_root6(double w) {
+    double q = (double)__powf((float)w, -1.0f / 6.0f);
+#pragma unroll
+    for (int it = 0; it < 2; it++) {
+        const double q2 = q * q;
+        const double q6 = q2 * q2 * q2;
+        q = fma(q * (1.0 / 6.0), fma(-w, q6, 1.0), q);
+    }
+    return q;
+}
+
+// ---------------------------------------------------------------------------
 // forward-mode dual number (value, tangent) for exact JVPs on the device
 // ---------------------------------------------------------------------------
 struct dual {
@@ -87,7 +151,7 @@ __device__ inline dual operator-(dual a, dual b) { return dual(a.v - b.v, a.d - 
 __device__ inline dual operator-(dual a) { return dual(-a.v, -a.d); }
 __device__ inline dual operator*(dual a, dual b) { return dual(a.v * b.v, fma(a.d, b.v, a.v * b.d)); }
 __device__ inline dual operator/(dual a, dual b) {
-    double r = 1.0 / b.v, q = a.v * r;
+    double r = nr_rcp(b.v), q = a.v * r;
     return dual(q, (a.d - q * b.d) * r);
 }
 __device__ inline dual operator+(dual a, double b) { return dual(a.v + b, a.d); }
@@ -96,7 +160,7 @@ __device__ inline dual operator-(dual a, double b) { return dual(a.v - b, a.d); 
 __device__ inline dual operator-(double b, dual a) { return dual(b - a.v, -a.d); }
 __device__ inline dual operator*(dual a, double b) { return dual(a.v * b, a.d * b); }
 __device__ inline dual operator*(double b, dual a) { return dual(a.v * b, a.d * b); }
-__device__ inline dual operator/(dual a, double b) { double r = 1.0 / b; return dual(a.v * r, a.d * r); }
+__device__ inline dual operator/(dual a, double b) { double r = nr_rcp(b); return dual(a.v * r, a.d * r); }
 __device__ inline bool operator>=(dual a, double b) { return a.v >= b; }
 __device__ inline bool operator>(dual a, double b) { return a.v > b; }
 __device__ inline bool operator<(dual a, double b) { return a.v < b; }
@@ -104,17 +168,32 @@ __device__ inline bool operator<(dual a, double b) { return a.v < b; }
 __device__ inline double val(double x) { return x; }
 __device__ inline double val(dual x) { return x.v; }
 
-__device__ inline double rcp(double x) { return 1.0 / x; }
-__device__ inline double tsqrt(double x) { return ::sqrt(x); }
+__device__ inline double rcp(double x) { return nr_rcp(x); }
+__device__ inline double tsqrt(double x) { return nr_sqrt(x); }
 __device__ inline double tfabs(double x) { return ::fabs(x); }
-__device__ inline dual rcp(dual x) { double r = 1.0 / x.v; return dual(r, -x.d * r * r); }
-__device__ inline dual tsqrt(dual x) { double s = ::sqrt(x.v); return dual(s, x.d * 0.5 / s); }
+__device__ inline dual rcp(dual x) { double r = nr_rcp(x.v); return dual(r, -x.d * r * r); }
+__device__ inline dual tsqrt(dual x) {
+    double y;
+    const double s = nr_sqrt_inv(x.v, &y);
+    return dual(s, x.d * 0.5 * y);
+}
+// sqrt(x) with 1/sqrt(x) in *inv
+__device__ inline double tsqrt_inv(double x, double* inv) { return nr_sqrt_inv(x, inv); }
+__device__ inline dual tsqrt_inv(dual x, dual* inv) {
+    double y;
+    const double s = nr_sqrt_inv(x.v, &y);
+    *inv = dual(y, -0.5 * x.d * y * y * y);
+    return dual(s, x.d * 0.5 * y);
+}
 __device__ inline dual tfabs(dual x) { return x.v < 0.0 ? -x : x; }
 __device__ inline double cbrt_(double x) { return ::cbrt(x); }
 __device__ inline dual cbrt_(dual x) { double c = ::cbrt(x.v); return dual(c, x.d * c / (3.0 * x.v)); }
-// x^(1/6) for x > 0
-__device__ inline double root6(double x) { return ::cbrt(::sqrt(x)); }
-__device__ inline dual root6(dual x) { double r = ::cbrt(::sqrt(x.v)); return dual(r, x.d * r / (6.0 * x.v)); }
+// x^(-1/6) for x > 0 (nr_inv_root6)
+__device__ inline double inv_root6(double x) { return nr_inv_root6(x); }
+__device__ inline dual inv_root6(dual x) {
+    const double q = nr_inv_root6(x.v), q2 = q * q;
+    return dual(q, x.d * (-1.0 / 6.0) * (q2 * q2 * q2 * q));  // d/dx x^(-1/6) = -(1/6) x^(-7/6)
+}
 
 template <class T> __device__ inline T tmin(T a, double b) { return val(a) < b ? a : T(b); }
 
@@ -123,10 +202,10 @@ template <class T> __device__ inline T tmin(T a, double b) { return val(a) < b ?
 template <class T>
 __device__ inline T laminar_mu(const DevCase& c, T temp) {
     if (c.law == 1) {
-        T tr = temp * (1.0 / c.T_inf);
+        T tr = temp * c.iT_inf;
         return c.mu_inf * tr * tsqrt(tr) * ((c.T_inf + c.suth_S) * rcp(temp + c.suth_S));
     }
-    T cb = cbrt_(temp * (1.0 / c.T_inf));
+    T cb = cbrt_(temp * c.iT_inf);
     return c.mu_inf * (cb * cb);
 }
 

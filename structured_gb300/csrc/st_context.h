@@ -61,6 +61,8 @@ struct st_ctx {
     double *strip_jac_d = nullptr, *strip_dt_d = nullptr, *strip_inv_d = nullptr, *strip_res_d = nullptr;
     const double* strip_W1 = nullptr;
     bool strip_ready = false;
+    double strip_host_ms = 0.0;   // host time of the last strip factorisation
+    int strip_factored = 0;       // strip factorisations since the context was made
     bool pfam_on[3] = {false, false, false};
     // learned SA correction: BF16 weights, FP32 biases + normalisation, FP32
     // master parameters with Adam moments, training partials

@@ -23,7 +23,7 @@ __global__ void __launch_bounds__(256) k_prim(DevCase c, const T* __restrict__ q
         T ri = rcp(rho);
         T u = Q[1] * ri, v = Q[2] * ri;
         T p = (Q[3] - 0.5 * rho * (u * u + v * v)) * GM1;
-        T temp = p * ri * (1.0 / c.R);
+        T temp = p * ri * c.iR;
         T nut = (NQ == 5) ? Q[NQ - 1] * ri : T(0.0);
         T mu = c.viscous ? laminar_mu(c, temp) : T(0.0);
         T mut = (NQ == 5 && c.viscous) ? sa_mut(rho, nut, mu) : T(0.0);
@@ -62,7 +62,7 @@ __device__ inline void bc_copy_nl(const DevCase& c, T* g, const T* s) {
 template <class T, int NQ>
 __device__ void bc_apply_block(const DevCase& c, T* __restrict__ P) {
     const int nic = c.nic, njc = c.njc;
-    const double iR = 1.0 / c.R;
+    const double iR = c.iR;
     for (int b = 0; b < c.nbc; b++) {
         const DevBC bc = c.bcs[b];
         const bool bt = (bc.face == 0 || bc.face == 2);
@@ -302,11 +302,12 @@ __device__ inline void roe_flux(T rlft, T ulft, T vlft, T plft, T rrht, T urht, 
     const T vav = (rat * vrht + vlft) * rati;
     const T hav = (rat * hrht + hlft) * rati;
     const T uv = 0.5 * (uav * uav + vav * vav);
-    const T cav = tsqrt(GM1 * (hav - uv));
+    T icav;
+    const T cav = tsqrt_inv(GM1 * (hav - uv), &icav);
     const T aq1 = rrht - rlft, aq2 = urht - ulft, aq3 = vrht - vlft, aq4 = prht - plft;
     const T uu = r1 * uav + r2 * vav;
     const T c2 = cav * cav;
-    const T c2i = rcp(c2);
+    const T c2i = icav * icav;
     const T auu = tfabs(uu);
     const T aupc = tfabs(uu + cav);
     const T aumc = tfabs(uu - cav);
@@ -435,9 +436,9 @@ __global__ void __launch_bounds__(256) k_face(DevCase c, const T* __restrict__ P
             if (NQ == 5) {
                 const T mutb = 0.375 * (pL[P_MUT] + pR[P_MUT]) + 0.0625 * (pPa[P_MUT] + pPb[P_MUT] + pMa[P_MUT] + pMb[P_MUT]);
                 mu = mub + mutb;
-                k = c.cp * (mub * (1.0 / c.pr) + mutb * (1.0 / PR_TURB));
+                k = mub * c.cp_pr + mutb * c.cp_prt;
             } else {
-                k = mub * (c.cp / c.pr);
+                k = mub * c.cp_pr;
             }
             const double nx = gm[G_NX], ny = gm[G_NY];
             const T tau_xy = mu * (dudy + dvdx);
@@ -470,29 +471,33 @@ __global__ void __launch_bounds__(256) k_face(DevCase c, const T* __restrict__ P
 // SA source per unit volume: rho (beta P - D) + (cb2/sigma) rho |grad nut|^2,
 // P = cb1 S~ nut, D = cw1 fw (nut/d)^2 (Spalart & Allmaras 1992, SA-noft2);
 // for nut < 0 (SA-neg) P = cb1 (1 - ct3) Omega nut, D = -cw1 (nut/d)^2.
+// fw = g ((1 + cw3^6) / (g^6 + cw3^6))^(1/6) is evaluated as
+// g (1 + cw3^6)^(1/6) (g^6 + cw3^6)^(-1/6), with one reciprocal per
+// quotient and the inverse sixth root by Newton's iteration.
 template <class T>
 __device__ inline T sa_source(T rho, T nut, T mu, double d, T omega, T gnut2, T beta) {
+    const double id2 = nr_rcp(d * d);
     if (val(nut) < 0.0)
-        return rho * (beta * (SA_CB1 * (1.0 - SA_CT3)) * omega * nut + SA_CW1 * (nut * nut) * (1.0 / (d * d)))
+        return rho * (beta * (SA_CB1 * (1.0 - SA_CT3)) * omega * nut + SA_CW1 * (nut * nut) * id2)
              + (SA_CB2 / SA_SIGMA) * rho * gnut2;
-    const double k2d2 = SA_KAPPA * SA_KAPPA * d * d;
+    const double ik2d2 = id2 * (1.0 / (SA_KAPPA * SA_KAPPA));
     const T chi = rho * nut * rcp(mu);
     const T chi3 = chi * chi * chi;
     const T fv1 = chi3 * rcp(chi3 + SA_CV1_3);
     const T fv2 = 1.0 - chi * rcp(1.0 + chi * fv1);
-    const T sbar = nut * fv2 * (1.0 / k2d2);
+    const T sbar = nut * fv2 * ik2d2;
     T stilde;
     if (val(sbar) >= -SA_CV2 * val(omega)) stilde = omega + sbar;
     else stilde = omega + omega * (SA_CV2 * SA_CV2 * omega + SA_CV3 * sbar) * rcp((SA_CV3 - 2.0 * SA_CV2) * omega - sbar);
     T r;
-    if (val(stilde) > 0.0) r = tmin(nut * rcp(stilde * k2d2), 10.0);
+    if (val(stilde) > 0.0) r = tmin(nut * rcp(stilde) * ik2d2, 10.0);
     else r = T(10.0);
     const T r2 = r * r;
     const T gg = r + SA_CW2 * (r2 * r2 * r2 - r);
     const T g2 = gg * gg;
-    const T fw = gg * root6((1.0 + SA_CW3_6) * rcp(g2 * g2 * g2 + SA_CW3_6));
+    const T fw = gg * (SA_C6 * inv_root6(g2 * g2 * g2 + SA_CW3_6));
     const T prod = beta * SA_CB1 * stilde * nut;
-    const T dest = SA_CW1 * fw * (nut * nut) * (1.0 / (d * d));
+    const T dest = SA_CW1 * fw * (nut * nut) * id2;
     return rho * (prod - dest) + (SA_CB2 / SA_SIGMA) * rho * gnut2;
 }
 

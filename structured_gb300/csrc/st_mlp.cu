@@ -250,6 +250,25 @@ __global__ void k_mlp_adam(const float* __restrict__ part, int nwarps, float lr,
     }
 }
 
+// Fixed-order reduction of the warps' partial gradients into the master
+// parameter layout (the same sums k_mlp_adam forms), without an update;
+// thread MP_N writes the batch loss.
+__global__ void k_mlp_grad_reduce(const float* __restrict__ part, int nwarps, float* __restrict__ grad) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p > MP_N) return;
+    int off;
+    if (p == MP_N) off = PT_LOSS;
+    else if (p < MP_B1) off = PT_W1 + ((p - MP_W1) / MLP_IN) * MLP_K1 + (p - MP_W1) % MLP_IN;
+    else if (p < MP_W2) off = PT_B1 + p - MP_B1;
+    else if (p < MP_B2) off = PT_W2 + p - MP_W2;
+    else if (p < MP_W3) off = PT_B2 + p - MP_B2;
+    else if (p < MP_B3) off = PT_W3 + p - MP_W3;
+    else off = PT_B3;
+    float g = 0.f;
+    for (int w = 0; w < nwarps; w++) g += part[(size_t)w * PT_N + off];
+    grad[p] = g;
+}
+
 // raw features of every cell (after a residual evaluation filled P and Gj)
 __global__ void k_sa_features(DevCase c, const double* __restrict__ P, const double* __restrict__ Gj,
                               float* __restrict__ out) {
@@ -396,6 +415,35 @@ int st_mlp_train(st_ctx* x, const float* feat_dev, const float* target_dev, long
         if (loss_host) ST_CUDA(cudaMemcpyAsync(loss_host + it, x->mlp_loss, sizeof(float), cudaMemcpyDeviceToHost, s));
     }
     ST_LAUNCH_CHECK("MLP training");
+    ST_CUDA(cudaStreamSynchronize(s));
+    return ST_OK;
+}
+
+int st_mlp_grad(st_ctx* x, const float* feat_dev, const float* target_dev, long n, int batch,
+                unsigned long long seed, int step, float* grad_host, float* loss_host) {
+    if (!x || !feat_dev || !target_dev || !grad_host) return fail(ST_ERR_ARG, "st_mlp_grad: null argument");
+    if (!x->mlp_wb) return fail(ST_ERR_ARG, "st_mlp_grad: no network (st_mlp_init first)");
+    if (n < 1 || step < 0 || batch < 32 || batch % (32 * TRAIN_WARPS) != 0)
+        return fail(ST_ERR_ARG, "st_mlp_grad: n >= 1, step >= 0 and batch a multiple of 64");
+    const int nwarps = batch / 32;
+    const size_t need = (size_t)nwarps * PT_N + MP_N + 1;  // partials, then the reduced gradient and loss
+    if (x->mlp_part_n < need) {
+        if (x->mlp_part) cudaFree(x->mlp_part);
+        x->mlp_part = nullptr;
+        x->mlp_part_n = 0;
+        if (cudaMalloc((void**)&x->mlp_part, need * sizeof(float)) != cudaSuccess)
+            return fail(ST_ERR_CUDA, "cudaMalloc (MLP gradient partials)");
+        x->mlp_part_n = need;
+    }
+    cudaStream_t s = x->stream;
+    float* g = x->mlp_part + (size_t)nwarps * PT_N;
+    k_mlp_train<<<nwarps / TRAIN_WARPS, TRAIN_WARPS * 32, 0, s>>>(feat_dev, target_dev, n, batch, seed, step,
+                                                                  (const __nv_bfloat16*)x->mlp_wb, x->mlp_wf,
+                                                                  x->mlp_part);
+    k_mlp_grad_reduce<<<(MP_N + 1 + 255) / 256, 256, 0, s>>>(x->mlp_part, nwarps, g);
+    ST_LAUNCH_CHECK("MLP gradient");
+    ST_CUDA(cudaMemcpyAsync(grad_host, g, MP_N * sizeof(float), cudaMemcpyDeviceToHost, s));
+    if (loss_host) ST_CUDA(cudaMemcpyAsync(loss_host, g + MP_N, sizeof(float), cudaMemcpyDeviceToHost, s));
     ST_CUDA(cudaStreamSynchronize(s));
     return ST_OK;
 }

@@ -9,7 +9,6 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
-#include <mutex>
 
 #include "st_context.h"
 
@@ -25,41 +24,39 @@ constexpr int NA_THREADS = 256;
 // different streams, or from different host threads) race on it.
 static __device__ __align__(256) double g_norm_scratch[NA_MAX_BLOCKS * NA_MAX_COMPONENTS];
 
-constexpr int NA_MAX_DEVICES = 64;
-double* g_scratch_addr[NA_MAX_DEVICES] = {};
-std::mutex g_scratch_mutex;
-
-// Device address of g_norm_scratch for the current device, looked up once per
-// device.  The host-side symbol is only a stand-in; kernels must receive the
-// address returned by cudaGetSymbolAddress.
+// Device address of g_norm_scratch in the current device's copy of this
+// module.  The host-side symbol is only a stand-in; kernels must receive the
+// address that cudaGetSymbolAddress returns.  It is looked up on every call
+// (a table lookup in the runtime, no allocation) rather than cached, so the
+// address stays valid after cudaDeviceReset or when the runtime reloads the
+// module in a new primary context.  The first lookup on a device loads the
+// module there; make that first call outside any stream capture.
 int scratch_address(double** out) {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return stx::cuda_fail(e, "st_norms_noalloc: cudaGetDevice");
-    if (dev < 0 || dev >= NA_MAX_DEVICES) return stx::fail(ST_ERR_ARG, "st_norms_noalloc: device index too large");
-    std::lock_guard<std::mutex> lock(g_scratch_mutex);
-    if (!g_scratch_addr[dev]) {
-        void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_norm_scratch);
-        if (e != cudaSuccess) return stx::cuda_fail(e, "st_norms_noalloc: cudaGetSymbolAddress");
-        g_scratch_addr[dev] = static_cast<double*>(p);
-    }
-    *out = g_scratch_addr[dev];
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_norm_scratch);
+    if (e != cudaSuccess) return stx::cuda_fail(e, "st_norms_noalloc: cudaGetSymbolAddress");
+    *out = static_cast<double*>(p);
     return ST_OK;
 }
 
 __global__ void __launch_bounds__(NA_THREADS) k_norm_partial_na(const double* __restrict__ r, size_t ncell, int nq,
                                                                 double* __restrict__ part) {
+    // fully unrolled with a guard on nq, so acc stays in registers
     double acc[NA_MAX_COMPONENTS];
+#pragma unroll
     for (int k = 0; k < NA_MAX_COMPONENTS; k++) acc[k] = 0.0;
     for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < ncell; idx += (size_t)gridDim.x * blockDim.x)
-        for (int k = 0; k < nq; k++) {
-            const double x = r[idx * nq + k];
-            acc[k] = fma(x, x, acc[k]);
-        }
+#pragma unroll
+        for (int k = 0; k < NA_MAX_COMPONENTS; k++)
+            if (k < nq) {
+                const double x = r[idx * nq + k];
+                acc[k] = fma(x, x, acc[k]);
+            }
     __shared__ double sm[NA_THREADS / 32][NA_MAX_COMPONENTS];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    for (int k = 0; k < nq; k++) {
+#pragma unroll
+    for (int k = 0; k < NA_MAX_COMPONENTS; k++) {
+        if (k >= nq) break;
         double x = acc[k];
         for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
         if (lane == 0) sm[wid][k] = x;

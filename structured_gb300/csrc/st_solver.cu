@@ -10,6 +10,7 @@
 // CFL / under-relaxation ramps (solver.cpp:198-236) and adds the tolerance exit
 // the reference has disabled (solver.cpp:145) plus a divergence guard.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -878,6 +879,7 @@ int check_err(st_ctx* x, const char* what) {
 // and invert its dense block on the host, upload the inverse.  A singular or
 // non-finite block leaves the plain ILU(0).
 int strip_factor(st_ctx* x, const LinOp& op, const double* j1) {
+    const auto t0 = std::chrono::steady_clock::now();
     const int nic = x->c.ni - 1, njc = x->c.nj - 1, nq = x->nq, ns = x->strip_ns, n = ns * nq;
     cudaStream_t s = x->stream;
     const size_t nb = (size_t)ns * NOFF * nq * nq;
@@ -898,6 +900,8 @@ int strip_factor(st_ctx* x, const LinOp& op, const double* j1) {
     ST_CUDA(cudaMemcpyAsync(x->strip_inv_d, inv.data(), inv.size() * 8, cudaMemcpyHostToDevice, s));
     ST_CUDA(cudaStreamSynchronize(s));
     x->strip_ready = true;
+    x->strip_factored++;
+    x->strip_host_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     return ST_OK;
 }
 
@@ -1318,6 +1322,16 @@ int st_tangent_solve_device(st_ctx* x, const double* b_dev, double* dq_dev, doub
     rc = factor_M(x, op);
     if (rc) return rc;
     return gmres(x, op, b_dev, dq_dev, krylov_m, maxit, rtol, stats);
+}
+
+int st_precond_info(st_ctx* x, int* strip_unknowns, int* strip_active, int* strip_factorisations,
+                    double* strip_host_ms) {
+    if (!x) return fail(ST_ERR_ARG, "st_precond_info: null context");
+    if (strip_unknowns) *strip_unknowns = x->strip_ns * x->nq;
+    if (strip_active) *strip_active = x->strip_ready ? 1 : 0;
+    if (strip_factorisations) *strip_factorisations = x->strip_factored;
+    if (strip_host_ms) *strip_host_ms = x->strip_host_ms;
+    return ST_OK;
 }
 
 }  // extern "C"

@@ -77,6 +77,7 @@ def load_library() -> ctypes.CDLL:
         "st_residual_vjp": (I, [V, _P, _P, _P, _P, I]),
         "st_fused_launch_count": (I, [V, I]),
         "st_probe_fp64": (I, [V, ctypes.POINTER(D)]),
+        "st_probe_nr_math": (I, [V, ctypes.c_longlong, V]),
         "st_last_kernel_ms": (I, [V, ctypes.POINTER(D), ctypes.POINTER(D)]),
         "st_profile_pipeline": (I, [V, I, I, _P, I, ctypes.c_char_p, I, ctypes.POINTER(I)]),
         "st_launch_counts": (I, [V, I, ctypes.POINTER(I), ctypes.POINTER(I)]),
@@ -99,8 +100,10 @@ def load_library() -> ctypes.CDLL:
         "st_mlp_set_normalization": (I, [V, V, V]),
         "st_mlp_enable": (I, [V, I]),
         "st_mlp_train": (I, [V, V, V, ctypes.c_long, I, I, ctypes.c_float, ctypes.c_ulonglong, V]),
+        "st_mlp_grad": (I, [V, V, V, ctypes.c_long, I, ctypes.c_ulonglong, I, V, V]),
         "st_sa_features": (I, [V, V]),
         "st_mlp_beta": (I, [V, V]),
+        "st_precond_info": (I, [V, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(D)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -384,6 +387,15 @@ def _eq_extras():
         rows = hist.reshape(-1, 1 + self.nq)
         return done.value, rows[rows[:, 0] > 0]
 
+    def precond_info(self) -> dict:
+        """Wake strip level of the implicit solve's preconditioner: its size,
+        whether the last factorisation built it, how often, host ms of the last."""
+        n, act, cnt, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+        _check(self.lib.st_precond_info(self.h, ctypes.byref(n), ctypes.byref(act), ctypes.byref(cnt),
+                                        ctypes.byref(ms)), "st_precond_info")
+        return {"strip_unknowns": n.value, "strip_active": bool(act.value), "strip_factorisations": cnt.value,
+                "strip_host_ms": ms.value}
+
     def wall_gradients(self) -> np.ndarray:
         """(u_x, u_y, v_x, v_y) at the j = 0 faces of the current state, [nic][4]."""
         out = np.empty((self.nic, 4))
@@ -420,6 +432,15 @@ def _eq_extras():
                                      float(lr), int(seed), _f32p(loss)), "st_mlp_train")
         return loss
 
+    def mlp_grad(self, feat_ptr, target_ptr, n: int, batch: int, seed: int, step: int = 0):
+        """Gradient (FP32 master layout) and loss of the batch st_mlp_train
+        draws at `step`, without an update."""
+        g = np.zeros(self.lib.st_mlp_param_count(), dtype=np.float32)
+        loss = np.zeros(1, dtype=np.float32)
+        _check(self.lib.st_mlp_grad(self.h, _vp(feat_ptr), _vp(target_ptr), int(n), int(batch), int(seed), int(step),
+                                    _f32p(g), _f32p(loss)), "st_mlp_grad")
+        return g, float(loss[0])
+
     def sa_features_device(self, out_ptr) -> None:
         _check(self.lib.st_sa_features(self.h, _vp(out_ptr)), "st_sa_features")
 
@@ -427,8 +448,8 @@ def _eq_extras():
         _check(self.lib.st_mlp_beta(self.h, _vp(out_ptr)), "st_mlp_beta")
 
     for f in (jacobian_assemble, jacobian_blocks, jacobian_apply_device, linear_solve_device, cf_gradient_device,
-              adjoint_solve_device, tangent_solve_device, explicit_solve, wall_gradients, mlp_init, mlp_params, mlp_set_params,
-              mlp_set_normalization, mlp_enable, mlp_train, sa_features_device, mlp_beta_device):
+              adjoint_solve_device, tangent_solve_device, explicit_solve, precond_info, wall_gradients, mlp_init, mlp_params, mlp_set_params,
+              mlp_set_normalization, mlp_enable, mlp_train, mlp_grad, sa_features_device, mlp_beta_device):
         setattr(EulerEquation, f.__name__, f)
 
 

@@ -20,12 +20,17 @@ def port_built():
     return True
 
 
+# Where the reference's sources are mounted (its src/ and examples/); the
+# STRUCTURED_REF environment variable overrides the default location.
+REF_ROOT = os.environ.get("STRUCTURED_REF", "/root/reference")
+
+
 @pytest.fixture(scope="session")
 def ref_available():
     """The reference build exists only where its sources are mounted."""
-    if not os.path.isdir("/root/reference/src"):
+    if not os.path.isdir(os.path.join(REF_ROOT, "src")):
         return False
-    r = subprocess.run(["make", "-s", "-j8", "-C", os.path.join(ROOT, "oracle"), "ref"])
+    r = subprocess.run(["make", "-s", "-j8", "-C", os.path.join(ROOT, "oracle"), "ref", "REF=" + REF_ROOT])
     return r.returncode == 0
 
 

@@ -14,9 +14,10 @@ GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 def golden_names():
     """Residual fixtures (the reference's calc_residual / calc_dt on a seeded
-    state); io_*.npz hold output files instead."""
+    state); io_*.npz hold output files and steady_*.npz converged states
+    instead."""
     return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz"))
-                  if not os.path.basename(p).startswith("io_"))
+                  if not os.path.basename(p).startswith(("io_", "steady_")))
 
 
 def load_golden(name: str):

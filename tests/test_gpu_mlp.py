@@ -87,8 +87,12 @@ def test_mlp_inference_matches_reference(gpu_lib, tmp_path):
     x = ((f - mean) * np.float32(1.0) / std).astype(np.float32)
     ref, _ = ref_forward(p, x)
     err = np.abs(b.cpu().numpy() - ref)
-    # FP32 accumulation order can move a BF16 rounding of an activation by one ulp
-    assert err.max() < 2e-2 and np.median(err) < 1e-4, (err.max(), np.median(err))
+    print("inference: max %.3e, median %.3e, max |beta| %.3f" % (err.max(), np.median(err), np.abs(ref).max()))
+    # The kernel rounds to BF16 where the restatement does; the two differ only
+    # where FP32 accumulation order moves an activation across a BF16 rounding
+    # boundary.  Bound: one BF16 ulp (2^-8 relative) of the largest beta.
+    assert err.max() <= 2.0 ** -8 * np.abs(ref).max(), (err.max(), np.median(err))
+    assert np.median(err) < 1e-5, np.median(err)
 
 
 def test_fused_beta_equals_beta_field(gpu_lib, tmp_path):
@@ -135,8 +139,10 @@ def test_mlp_training_step_and_convergence(gpu_lib, tmp_path):
     ft = torch.tensor(feat, device="cuda")
     tt = torch.tensor(target, device="cuda")
     batch, seed = 256, 12345
+    g_gpu, loss0 = eq.mlp_grad(ft.data_ptr(), tt.data_ptr(), n, batch, seed, step=0)
     loss1 = eq.mlp_train(ft.data_ptr(), tt.data_ptr(), n, 1, batch=batch, lr=1e-3, seed=seed)
     p1 = eq.mlp_params()
+    assert loss0 == float(loss1[0])
     # numpy gradient on the same samples
     slot = np.arange(batch, dtype=np.uint64)
     idx = (splitmix64(np.uint64(seed) ^ splitmix64(np.uint64(0) * np.uint64(batch) + slot)) % np.uint64(n)).astype(np.int64)
@@ -148,10 +154,24 @@ def test_mlp_training_step_and_convergence(gpu_lib, tmp_path):
     d2 = bf16(dy[:, None] * bf16(w3)[None, :] * (1 - h2 ** 2))
     d1 = bf16((d2 @ bf16(W2)) * (1 - h1 ** 2))
     g = np.concatenate([(d1.T @ xb).ravel(), d1.sum(0), (d2.T @ h1).ravel(), d2.sum(0), h2.T @ dy, [dy.sum()]])
+    # the training kernels' gradient in value: BF16 rounding of the backward
+    # activations happens at the same points; FP32 accumulation order can move
+    # a rounding by one BF16 ulp (2^-8 relative), which the bound allows per
+    # entry on top of 1e-3 of the largest entry
+    gmax = np.abs(g).max()
+    err = np.abs(g_gpu - g)
+    big = np.abs(g) > 1e-2 * gmax
+    rel = err[big] / np.abs(g[big])
+    print("gradient: max rel %.3e on %d entries above 1e-2 max, median %.3e; max abs / max %.3e"
+          % (rel.max(), big.sum(), np.median(rel), err.max() / gmax))
+    assert (err <= 2.0 ** -8 * np.abs(g) + 1e-3 * gmax).all(), (err / (np.abs(g) + 1e-3 * gmax)).max()
+    assert np.median(rel) < 1e-3
+    # the first Adam step from zero moments is -lr g / (|g| + 1e-8) of the
+    # kernels' own gradient (bias-corrected moments g and g^2)
     step = p1 - p0
-    big = np.abs(g) > 1e-2 * np.abs(g).max()
-    agree = (np.sign(step[big]) == -np.sign(g[big])).mean()
-    assert agree > 0.98, agree
+    expect = -1e-3 * g_gpu / (np.abs(g_gpu) + 1e-8)
+    tol = 2e-7 + 4 * np.finfo(np.float32).eps * np.abs(p0).max()  # rounding of p0 - lr (...) in FP32
+    assert np.abs(step - expect).max() <= tol, np.abs(step - expect).max()
     # a learnable target: the loss falls by an order of magnitude
     loss = eq.mlp_train(ft.data_ptr(), tt.data_ptr(), n, 400, batch=4096, lr=3e-3, seed=seed + 1)
     assert loss[-20:].mean() < 0.1 * loss[:5].mean(), (loss[:5], loss[-5:])

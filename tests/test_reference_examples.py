@@ -12,9 +12,10 @@ import numpy as np
 import pytest
 
 import block_jacobian as BJ
+from conftest import REF_ROOT
 from structured_gb300 import case as C
 
-EXAMPLES = "/root/reference/examples/laminar"
+EXAMPLES = os.path.join(REF_ROOT, "examples", "laminar")
 CASES = [("naca0012", "config.inp"), ("channel", "implicit.inp"), ("channel", "explicit.inp")]
 
 
