@@ -168,15 +168,18 @@ __device__ inline bool operator<(dual a, double b) { return a.v < b; }
 __device__ inline double val(double x) { return x; }
 __device__ inline double val(dual x) { return x.v; }
 
-__device__ inline double rcp(double x) { return nr_rcp(x); }
-__device__ inline double tsqrt(double x) { return nr_sqrt(x); }
+// rcp / tsqrt: IEEE-rounded reciprocal and square root.  frcp: the
+// Newton-Raphson reciprocal above.  Measured per kernel on this part (one
+// fused residual + adjoint step at 4097x2049): frcp is the faster one in the
+// cell-wise passes (primitives, limiter, SA source), the IEEE forms in the
+// register-capped face passes.
+__device__ inline double rcp(double x) { return 1.0 / x; }
+__device__ inline double tsqrt(double x) { return ::sqrt(x); }
 __device__ inline double tfabs(double x) { return ::fabs(x); }
-__device__ inline dual rcp(dual x) { double r = nr_rcp(x.v); return dual(r, -x.d * r * r); }
-__device__ inline dual tsqrt(dual x) {
-    double y;
-    const double s = nr_sqrt_inv(x.v, &y);
-    return dual(s, x.d * 0.5 * y);
-}
+__device__ inline dual rcp(dual x) { double r = 1.0 / x.v; return dual(r, -x.d * r * r); }
+__device__ inline dual tsqrt(dual x) { double s = ::sqrt(x.v); return dual(s, x.d * 0.5 / s); }
+__device__ inline double frcp(double x) { return nr_rcp(x); }
+__device__ inline dual frcp(dual x) { double r = nr_rcp(x.v); return dual(r, -x.d * r * r); }
 // sqrt(x) with 1/sqrt(x) in *inv
 __device__ inline double tsqrt_inv(double x, double* inv) { return nr_sqrt_inv(x, inv); }
 __device__ inline dual tsqrt_inv(dual x, dual* inv) {
@@ -203,7 +206,7 @@ template <class T>
 __device__ inline T laminar_mu(const DevCase& c, T temp) {
     if (c.law == 1) {
         T tr = temp * c.iT_inf;
-        return c.mu_inf * tr * tsqrt(tr) * ((c.T_inf + c.suth_S) * rcp(temp + c.suth_S));
+        return c.mu_inf * tr * tsqrt(tr) * ((c.T_inf + c.suth_S) * frcp(temp + c.suth_S));
     }
     T cb = cbrt_(temp * c.iT_inf);
     return c.mu_inf * (cb * cb);
@@ -214,9 +217,9 @@ __device__ inline T laminar_mu(const DevCase& c, T temp) {
 template <class T>
 __device__ inline T sa_mut(T rho, T nut, T mu) {
     if (val(nut) < 0.0) return T(0.0);
-    T chi = rho * nut * rcp(mu);
+    T chi = rho * nut * frcp(mu);
     T chi3 = chi * chi * chi;
-    return rho * nut * (chi3 * rcp(chi3 + SA_CV1_3));
+    return rho * nut * (chi3 * frcp(chi3 + SA_CV1_3));
 }
 
 // The nu_tilde part of the SA diffusion coefficient, rho nu_tilde f_n(chi):

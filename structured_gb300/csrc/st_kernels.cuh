@@ -20,7 +20,7 @@ __global__ void __launch_bounds__(256) k_prim(DevCase c, const T* __restrict__ q
         const int i = (int)(idx / c.njc), j = (int)(idx % c.njc);
         const T* Q = q + idx * NQ;
         T rho = Q[0];
-        T ri = rcp(rho);
+        T ri = frcp(rho);
         T u = Q[1] * ri, v = Q[2] * ri;
         T p = (Q[3] - 0.5 * rho * (u * u + v * v)) * GM1;
         T temp = p * ri * c.iR;
@@ -221,7 +221,7 @@ __global__ void __launch_bounds__(256) k_limiter(DevCase c, const T* __restrict_
                 const int m = slot[k];
                 const T fa = pc[m] - pm[m], fb = pp[m] - pc[m];
                 const T a1 = 3.0 * fb * fa;
-                const T inv = rcp(2.0 * (fb - fa) * (fb - fa) + a1 + eps);
+                const T inv = frcp(2.0 * (fb - fa) * (fb - fa) + a1 + eps);
                 const T ph = 0.25 * (a1 + eps) * inv;
                 const T tl = THM * fa + THP * fb, tr = THP * fa + THM * fb;
                 lim[lim_off(c, dir, LIM_SL, idx) + k] = ph * tl;
@@ -481,16 +481,16 @@ __device__ inline T sa_source(T rho, T nut, T mu, double d, T omega, T gnut2, T 
         return rho * (beta * (SA_CB1 * (1.0 - SA_CT3)) * omega * nut + SA_CW1 * (nut * nut) * id2)
              + (SA_CB2 / SA_SIGMA) * rho * gnut2;
     const double ik2d2 = id2 * (1.0 / (SA_KAPPA * SA_KAPPA));
-    const T chi = rho * nut * rcp(mu);
+    const T chi = rho * nut * frcp(mu);
     const T chi3 = chi * chi * chi;
-    const T fv1 = chi3 * rcp(chi3 + SA_CV1_3);
-    const T fv2 = 1.0 - chi * rcp(1.0 + chi * fv1);
+    const T fv1 = chi3 * frcp(chi3 + SA_CV1_3);
+    const T fv2 = 1.0 - chi * frcp(1.0 + chi * fv1);
     const T sbar = nut * fv2 * ik2d2;
     T stilde;
     if (val(sbar) >= -SA_CV2 * val(omega)) stilde = omega + sbar;
-    else stilde = omega + omega * (SA_CV2 * SA_CV2 * omega + SA_CV3 * sbar) * rcp((SA_CV3 - 2.0 * SA_CV2) * omega - sbar);
+    else stilde = omega + omega * (SA_CV2 * SA_CV2 * omega + SA_CV3 * sbar) * frcp((SA_CV3 - 2.0 * SA_CV2) * omega - sbar);
     T r;
-    if (val(stilde) > 0.0) r = tmin(nut * rcp(stilde) * ik2d2, 10.0);
+    if (val(stilde) > 0.0) r = tmin(nut * frcp(stilde) * ik2d2, 10.0);
     else r = T(10.0);
     const T r2 = r * r;
     const T gg = r + SA_CW2 * (r2 * r2 * r2 - r);
