@@ -310,9 +310,17 @@ def run_ours(args, world, rank, local):
     ms_step = el_ms / args.steps
     value = job_rate(world, cells, args.steps, el_ms * 1e-3)
 
-    # per-launch attribution (outside the timed region)
+    # per-launch attribution (outside the timed region): the residual by the
+    # default (tiled, TMA-staged) sweeps and, for comparison, by the per-stage passes
     kern_res = eq.profile("residual")
     res_ms = float(sum(kern_res.values()))
+    kern_res_stage = None
+    try:
+        eq.set_residual_path(False)
+        kern_res_stage = eq.profile("residual")
+        eq.set_residual_path(True)
+    except StructuredError:
+        pass
     kern_adj = eq.profile("fused") if with_adj else {}
     adj_ms = float(sum(kern_adj.values()))
     fp64_peak = eq.probe_fp64_tflops()
@@ -364,6 +372,7 @@ def run_ours(args, world, rank, local):
     prof = ("residual_adjoint_%s_%s.md" if with_adj else "residual_%s_%s.md") % (tb, args.grid)
     traffic_cell = profile_figure(prof, "dram_bytes_per_cell")
     flops_cell = profile_figure(prof, "fp64_flops_per_cell")
+    pipe_pct = profile_figure(prof, "fp64_pipe_active_pct")
     kern = kern_adj if with_adj else kern_res
     top = max(kern, key=kern.get) if kern else None
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
@@ -371,7 +380,7 @@ def run_ours(args, world, rank, local):
             "traffic": traffic_cell * cells if traffic_cell else None,
             "scope": "whole %s evaluation (%d launches), %d algorithmic B/cell"
                      % ("fused residual+adjoint" if with_adj else "residual", kernels_per_step, alg),
-            "kernels_ms": {"residual": kern_res, "adjoint": kern_adj}}
+            "kernels_ms": {"residual": kern_res, "residual_per_stage": kern_res_stage, "adjoint": kern_adj}}
     if top:
         roof["dominant_kernel"] = {"name": top, "ms": kern[top], "share": kern[top] / max(sum(kern.values()), 1e-30)}
     if flops_cell:
@@ -379,7 +388,9 @@ def run_ours(args, world, rank, local):
         roof["fp64"] = {"scope": "%s pipeline (ncu-counted flops / event time)"
                                  % ("fused residual+adjoint" if with_adj else "residual"),
                         "achieved_tflops": fp64_ach, "peak_tflops": fp64_peak, "frac": fp64_ach / fp64_peak,
-                        "flops_per_cell": flops_cell, "peak_source": "live DFMA probe (st_probe_fp64)"}
+                        "flops_per_cell": flops_cell, "peak_source": "live DFMA probe (st_probe_fp64)",
+                        "pipe_active_frac": pipe_pct / 100.0 if pipe_pct else None,
+                        "pipe_source": "ncu sm__pipe_fp64_cycles_active, time-weighted over the step (profiles/)"}
     else:
         roof["fp64"] = {"peak_tflops": fp64_peak, "peak_source": "live DFMA probe (st_probe_fp64)"}
     line = {"metric": metric_name(with_adj), "value": value, "unit": "Mcells/s", "n_gpus": world,
@@ -388,6 +399,10 @@ def run_ours(args, world, rank, local):
             "config": workload_config(args, args.grid), "roofline": roof, "e2e": e2e,
             "clocks": clk.summary(), "gpu_launches": kernels_per_step * args.steps,
             "breakdown": rate_breakdown(cells, res_ms, adj_ms if with_adj else None)}
+    if kern_res_stage:
+        st_ms = float(sum(kern_res_stage.values()))
+        line["breakdown"]["residual_per_stage"] = cells / (st_ms * 1e-3) / 1e6
+        line["breakdown"]["residual_per_stage_ms"] = st_ms
     if world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_sample(tb, 12.0, os.cpu_count() or 1, with_adj)
     print(json.dumps(line), flush=True)

@@ -133,6 +133,17 @@ int st_residual(st_ctx* ctx, int lhs, double* rhs_host);
 int st_residual_device(st_ctx* ctx, const double* q_dev, const double* beta_dev,
                        double* rhs_dev, int lhs);
 
+/* Which kernels evaluate the FP64 residual of st_residual*, the Newton and
+ * explicit solvers: path 1 (the default where available) = tiled i- and
+ * j-sweeps whose CTAs stage their tile of primitive records plus a two-cell
+ * halo in shared memory by TMA and keep slopes and face fluxes on chip;
+ * path 0 = one pass per stage (slopes, i-faces, j-faces, cells) through HBM.
+ * Both compute the stages of calc_residual (eulerequation.cpp:168-232) with
+ * the same face arithmetic.  The network-beta residual and JVPs always use the
+ * per-stage passes.  *active (may be NULL) = 1 if the tiled sweeps now run.
+ * ST_ERR_UNSUPPORTED for path 1 when the driver offers no tensor-map encoder. */
+int st_set_residual_path(st_ctx* ctx, int path, int* active);
+
 /* Local time step: EulerEquation::calc_dt(cfl), eulerequation.cpp:237-259.
  * dt_host [nic][njc][nq] may be NULL. */
 int st_dt(st_ctx* ctx, double cfl, double* dt_host);
@@ -142,9 +153,13 @@ int st_norms(st_ctx* ctx, double* out);
 
 /* Wall skin friction at the j=0 faces, the reference's
  * Cf = mu_inf (du/dy - dv/dx)/q_inf (IOManager::write_surface,
- * src/utils/io.cpp:217-226), of the current state; cf_host [nic].  J is
- * sum Cf dx over plate faces with x <= plate_x_end. */
+ * src/utils/io.cpp:217-226), of the current state; cf_host [nic] (may be
+ * NULL).  J is sum Cf dx over plate faces with x <= plate_x_end, reduced on
+ * the device (warp-shuffle tree, fixed order). */
 int st_skin_friction(st_ctx* ctx, double* cf_host, double* J);
+/* Same on the device without synchronising: cf_dev [nic] and J_dev [1]
+ * (either may be NULL) are written on the context stream. */
+int st_skin_friction_device(st_ctx* ctx, double* cf_dev, double* J_dev);
 /* Velocity gradients (u_x, u_y, v_x, v_y) of the current state at the j = 0
  * faces, [nic][4] on the host: the row of the reference's grad_u_eta /
  * grad_v_eta that IOManager::write_surface reads for Cf and the viscous

@@ -13,6 +13,7 @@
 
 #include "st_context.h"
 #include "st_kernels.cuh"
+#include "st_tile.cuh"
 
 using namespace st;
 
@@ -147,41 +148,57 @@ void host_geometry(st_ctx* x, std::vector<double>& gi, std::vector<double>& gj) 
 
 // Wall distance: nearest point on any bottom no-slip wall segment, brute force
 // over segments staged in shared memory.
-__global__ void k_wall_distance(int nic, int njc, int nj, const double* xv, const double* yv,
-                                const int* seg, int nseg, double* wd) {
-    __shared__ double s[4][256];
+// Distance from each cell centre to the nearest no-slip wall segment (exact
+// minimum over every segment).  Segments come in chunks of WD_CHUNK in wall
+// order with the chunk's bounding box; a chunk is scanned only if the squared
+// distance from the point to its box (a lower bound for every segment in it,
+// with a relative margin for rounding) does not exceed the best so far, so the
+// minimum is the brute-force one while most chunks are skipped.  The first
+// chunk scanned is the one holding the cell's own column when that column is
+// on the wall (a tight starting bound for body-fitted grids).
+constexpr int WD_CHUNK = 32;
+__device__ inline double seg_dist2(double px, double py, double x0, double y0, double x1, double y1) {
+    const double ax = x1 - x0, ay = y1 - y0;
+    const double wx = px - x0, wy = py - y0;
+    const double l2 = ax * ax + ay * ay;
+    double t = l2 > 0.0 ? (wx * ax + wy * ay) / l2 : 0.0;
+    t = fmin(1.0, fmax(0.0, t));
+    const double dx = wx - t * ax, dy = wy - t * ay;
+    return dx * dx + dy * dy;
+}
+__global__ void k_wall_distance(int nic, int njc, int nj, const double* __restrict__ xv, const double* __restrict__ yv,
+                                const int* __restrict__ seg, int nseg, const double* __restrict__ cbox,
+                                const int* __restrict__ col_chunk, double* __restrict__ wd) {
     const size_t n = (size_t)nic * njc;
-    const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    double px = 0, py = 0;
-    if (idx < n) {
-        int i = (int)(idx / njc), j = (int)(idx % njc);
-        px = 0.25 * (xv[(size_t)i * nj + j] + xv[(size_t)(i + 1) * nj + j] + xv[(size_t)i * nj + j + 1] + xv[(size_t)(i + 1) * nj + j + 1]);
-        py = 0.25 * (yv[(size_t)i * nj + j] + yv[(size_t)(i + 1) * nj + j] + yv[(size_t)i * nj + j + 1] + yv[(size_t)(i + 1) * nj + j + 1]);
-    }
-    double best = 1e300;
-    for (int base = 0; base < nseg; base += 256) {
-        __syncthreads();
-        int sidx = base + threadIdx.x;
-        if (sidx < nseg) {
-            int i = seg[sidx];
-            s[0][threadIdx.x] = xv[(size_t)i * nj];
-            s[1][threadIdx.x] = yv[(size_t)i * nj];
-            s[2][threadIdx.x] = xv[(size_t)(i + 1) * nj];
-            s[3][threadIdx.x] = yv[(size_t)(i + 1) * nj];
+    for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += (size_t)gridDim.x * blockDim.x) {
+        const int i = (int)(idx / njc), j = (int)(idx % njc);
+        const double px = 0.25 * (xv[(size_t)i * nj + j] + xv[(size_t)(i + 1) * nj + j] + xv[(size_t)i * nj + j + 1] +
+                                  xv[(size_t)(i + 1) * nj + j + 1]);
+        const double py = 0.25 * (yv[(size_t)i * nj + j] + yv[(size_t)(i + 1) * nj + j] + yv[(size_t)i * nj + j + 1] +
+                                  yv[(size_t)(i + 1) * nj + j + 1]);
+        double best = 1e300;
+        const int nch = (nseg + WD_CHUNK - 1) / WD_CHUNK;
+        auto scan = [&](int ch) {
+            const int k1 = min(nseg, (ch + 1) * WD_CHUNK);
+            for (int k = ch * WD_CHUNK; k < k1; k++) {
+                const int s = seg[k];
+                best = fmin(best, seg_dist2(px, py, xv[(size_t)s * nj], yv[(size_t)s * nj], xv[(size_t)(s + 1) * nj],
+                                            yv[(size_t)(s + 1) * nj]));
+            }
+        };
+        const int first = col_chunk[i];
+        if (first >= 0) scan(first);
+        for (int ch = 0; ch < nch; ch++) {
+            if (ch == first) continue;
+            const double* b = cbox + ch * 4;  // xmin, ymin, xmax, ymax
+            const double dx = fmax(0.0, fmax(b[0] - px, px - b[2]));
+            const double dy = fmax(0.0, fmax(b[1] - py, py - b[3]));
+            const double lb = dx * dx + dy * dy;
+            if (lb * (1.0 - 1e-12) > best) continue;
+            scan(ch);
         }
-        __syncthreads();
-        int cnt = min(256, nseg - base);
-        for (int k = 0; k < cnt; k++) {
-            double ax = s[2][k] - s[0][k], ay = s[3][k] - s[1][k];
-            double wx = px - s[0][k], wy = py - s[1][k];
-            double l2 = ax * ax + ay * ay;
-            double t = l2 > 0.0 ? (wx * ax + wy * ay) / l2 : 0.0;
-            t = fmin(1.0, fmax(0.0, t));
-            double dx = wx - t * ax, dy = wy - t * ay;
-            best = fmin(best, dx * dx + dy * dy);
-        }
+        wd[idx] = nseg ? ::sqrt(best) : 1e30;
     }
-    if (idx < n) wd[idx] = nseg ? ::sqrt(best) : 1e30;
 }
 
 // ---------------------------------------------------------------------------
@@ -247,6 +264,24 @@ __global__ void k_skin_friction(DevCase c, const double* __restrict__ P, double 
     double uy = gm[G_WLY] * pL[P_U] + gm[G_WRY] * pR[P_U] + gm[G_WPY] * (a[P_U] + b[P_U]) + gm[G_WMY] * (m[P_U] + n[P_U]);
     double vx = gm[G_WLX] * pL[P_V] + gm[G_WRX] * pR[P_V] + gm[G_WPX] * (a[P_V] + b[P_V]) + gm[G_WMX] * (m[P_V] + n[P_V]);
     cf[i] = c.mu_inf * (uy - vx) / qinf;
+}
+
+// J = sum_i w_i Cf_i over the wall faces, one CTA: strided partial sums,
+// warp-shuffle tree, then the eight warp sums in a fixed order
+// (deterministic).  out[0] = J.
+__global__ void __launch_bounds__(256) k_drag(const double* __restrict__ cf, const double* __restrict__ w, int n,
+                                              double* __restrict__ out) {
+    double acc = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) acc = fma(cf[i], w[i], acc);
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    __shared__ double sm[8];
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int k = 0; k < 8; k++) s += sm[k];
+        out[0] = s;
+    }
 }
 
 // velocity gradients (u_x, u_y, v_x, v_y) at the j = 0 faces, the row of
@@ -350,6 +385,75 @@ int launch_forward(st_ctx* x, const DevCase& dc, const T* q, const T* beta, T* P
     return ST_OK;
 }
 
+// Residual by the tiled sweeps: primitives and boundary ghosts as in the
+// per-face pipeline, then one TMA-staged i-sweep and one j-sweep.
+template <int NQ>
+int launch_tiled(st_ctx* x, const double* q, const double* beta, double* rhs, int order) {
+    cudaStream_t s = x->stream;
+    const DevCase& dc = x->dc;
+    const int nic = x->c.ni - 1, njc = x->c.nj - 1;
+    k_prim<double, NQ><<<grid_for(x->ncell), 256, 0, s>>>(dc, q, x->P);
+    stx::mark(x, "k_prim");
+    k_bc<double, NQ><<<1, 1024, 0, s>>>(dc, x->P);
+    stx::mark(x, "k_bc");
+    const dim3 gi((nic + TI_I - 1) / TI_I, (njc + TJ_I - 1) / TJ_I);
+    const dim3 gj((njc + TJ_J - 1) / TJ_J, (nic + TI_J - 1) / TI_J);
+    if (order == 2) {
+        k_sweep_i<NQ, 2><<<gi, SW_THREADS, SWEEP_SMEM_I, s>>>(dc, x->tmap_i, rhs, x->Gi);
+        stx::mark(x, "k_sweep_i");
+        k_sweep_j<NQ, 2><<<gj, SW_THREADS, SWEEP_SMEM_J, s>>>(dc, x->tmap_j, x->Gi, beta, rhs);
+    } else {
+        k_sweep_i<NQ, 1><<<gi, SW_THREADS, SWEEP_SMEM_I, s>>>(dc, x->tmap_i, rhs, x->Gi);
+        stx::mark(x, "k_sweep_i");
+        k_sweep_j<NQ, 1><<<gj, SW_THREADS, SWEEP_SMEM_J, s>>>(dc, x->tmap_j, x->Gi, beta, rhs);
+    }
+    stx::mark(x, "k_sweep_j");
+    ST_LAUNCH_CHECK("tiled residual launch");
+    return ST_OK;
+}
+
+// TMA descriptors of P = [nic+2][njc+2][8] doubles (innermost first: record
+// slot, padded j, padded i) for the two sweep boxes, and the sweeps' dynamic
+// shared memory limits.  Leaves tile_ok false (the per-face passes then run)
+// if the driver entry point or an encoding is unavailable.
+int setup_tiles(st_ctx* x) {
+    x->tile_ok = false;
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !fn) {
+        cudaGetLastError();
+        return ST_OK;
+    }
+    auto encode = reinterpret_cast<CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                                const cuuint64_t*, const cuuint32_t*, const cuuint32_t*,
+                                                CUtensorMapInterleave, CUtensorMapSwizzle, CUtensorMapL2promotion,
+                                                CUtensorMapFloatOOBfill)>(fn);
+    const int nic = x->c.ni - 1, njc = x->c.nj - 1;
+    const cuuint64_t dims[3] = {(cuuint64_t)NP, (cuuint64_t)(njc + 2), (cuuint64_t)(nic + 2)};
+    const cuuint64_t strides[2] = {(cuuint64_t)NP * 8, (cuuint64_t)(njc + 2) * NP * 8};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    const cuuint32_t box_i[3] = {(cuuint32_t)NP, (cuuint32_t)BJ_I, (cuuint32_t)BI_I};
+    const cuuint32_t box_j[3] = {(cuuint32_t)NP, (cuuint32_t)BJ_J, (cuuint32_t)BI_J};
+    if (reinterpret_cast<uintptr_t>(x->P) % 16) return ST_OK;
+    for (int w = 0; w < 2; w++) {
+        CUresult r = encode(w == 0 ? &x->tmap_i : &x->tmap_j, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, x->P, dims, strides,
+                            w == 0 ? box_i : box_j, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS) return ST_OK;
+    }
+    ST_CUDA(cudaFuncSetAttribute(k_sweep_i<5, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SWEEP_SMEM_I));
+    ST_CUDA(cudaFuncSetAttribute(k_sweep_i<5, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SWEEP_SMEM_I));
+    ST_CUDA(cudaFuncSetAttribute(k_sweep_i<4, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SWEEP_SMEM_I));
+    ST_CUDA(cudaFuncSetAttribute(k_sweep_i<4, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SWEEP_SMEM_I));
+    ST_CUDA(cudaFuncSetAttribute(k_sweep_j<5, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SWEEP_SMEM_J));
+    ST_CUDA(cudaFuncSetAttribute(k_sweep_j<5, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SWEEP_SMEM_J));
+    ST_CUDA(cudaFuncSetAttribute(k_sweep_j<4, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SWEEP_SMEM_J));
+    ST_CUDA(cudaFuncSetAttribute(k_sweep_j<4, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SWEEP_SMEM_J));
+    x->tile_ok = true;
+    return ST_OK;
+}
+
 int order_of(st_ctx* x, int lhs) { return lhs ? x->c.lhs_order : x->c.order; }
 
 }  // namespace
@@ -415,6 +519,12 @@ int run_norms(st_ctx* x, const double* rhs, double* out) {
 }
 
 int run_residual(st_ctx* x, const double* q, const double* beta, double* rhs, int order) {
+    if (x->tile_ok && x->res_path == 1 && !x->dc.mlp_wb)
+        return x->nq == 5 ? launch_tiled<5>(x, q, beta, rhs, order) : launch_tiled<4>(x, q, beta, rhs, order);
+    return run_residual_faces(x, q, beta, rhs, order);
+}
+
+int run_residual_faces(st_ctx* x, const double* q, const double* beta, double* rhs, int order) {
     if (x->nq == 5)
         return launch_forward<double, 5>(x, x->dc, q, beta, x->P, x->lim, x->Fi, x->Fj, x->Gi, x->Gj, rhs, order);
     return launch_forward<double, 4>(x, x->dc, q, beta, x->P, x->lim, x->Fi, x->Fj, x->Gi, x->Gj, rhs, order);
@@ -513,6 +623,7 @@ int st_create(const st_case* c, const double* xv, const double* yv, int device, 
     cudaMemset(x->Gj, 0, x->nfj * 4 * 8);
     cudaMemset(x->err_d, 0, sizeof(int));
     k_fill<<<grid_for(x->ncell), 256, 0, x->stream>>>(x->beta, x->ncell, 1.0);
+    if (int rt = setup_tiles(x)) { st_destroy(x); return rt; }
 
     // wall distance (no-slip bottom segments, last writer wins per column)
     {
@@ -526,17 +637,38 @@ int st_create(const st_case* c, const double* xv, const double* yv, int device, 
         }
         std::vector<int> seg;
         for (int i = 0; i < nic; i++) if (wall[i]) seg.push_back(i);
-        double *xv_d = nullptr, *yv_d = nullptr; int* seg_d = nullptr;
+        // chunk bounding boxes (wall order) and each column's own chunk
+        const int nch = (int)((seg.size() + WD_CHUNK - 1) / WD_CHUNK);
+        std::vector<double> cbox((size_t)std::max(1, nch) * 4);
+        std::vector<int> col_chunk(nic, -1);
+        for (int ch = 0; ch < nch; ch++) {
+            double b[4] = {1e300, 1e300, -1e300, -1e300};
+            for (size_t k = (size_t)ch * WD_CHUNK; k < std::min(seg.size(), (size_t)(ch + 1) * WD_CHUNK); k++) {
+                col_chunk[seg[k]] = ch;
+                for (int e = 0; e < 2; e++) {
+                    const double px = x->xv[(size_t)(seg[k] + e) * nj], py = x->yv[(size_t)(seg[k] + e) * nj];
+                    b[0] = std::min(b[0], px); b[1] = std::min(b[1], py);
+                    b[2] = std::max(b[2], px); b[3] = std::max(b[3], py);
+                }
+            }
+            for (int e = 0; e < 4; e++) cbox[(size_t)ch * 4 + e] = b[e];
+        }
+        double *xv_d = nullptr, *yv_d = nullptr, *cbox_d = nullptr; int *seg_d = nullptr, *col_d = nullptr;
         rc = alloc(&xv_d, x->xv.size());
         if (rc == ST_OK) rc = alloc(&yv_d, x->yv.size());
         if (rc == ST_OK) rc = alloc(&seg_d, std::max<size_t>(1, seg.size()));
+        if (rc == ST_OK) rc = alloc(&cbox_d, cbox.size());
+        if (rc == ST_OK) rc = alloc(&col_d, (size_t)nic);
         if (rc != ST_OK) { st_destroy(x); return rc; }
         cudaMemcpy(xv_d, x->xv.data(), x->xv.size() * 8, cudaMemcpyHostToDevice);
         cudaMemcpy(yv_d, x->yv.data(), x->yv.size() * 8, cudaMemcpyHostToDevice);
         if (!seg.empty()) cudaMemcpy(seg_d, seg.data(), seg.size() * sizeof(int), cudaMemcpyHostToDevice);
-        k_wall_distance<<<grid_for(x->ncell), 256, 0, x->stream>>>(nic, njc, nj, xv_d, yv_d, seg_d, (int)seg.size(), x->wd);
+        cudaMemcpy(cbox_d, cbox.data(), cbox.size() * 8, cudaMemcpyHostToDevice);
+        cudaMemcpy(col_d, col_chunk.data(), (size_t)nic * sizeof(int), cudaMemcpyHostToDevice);
+        k_wall_distance<<<grid_for(x->ncell), 256, 0, x->stream>>>(nic, njc, nj, xv_d, yv_d, seg_d, (int)seg.size(),
+                                                                   cbox_d, col_d, x->wd);
         cudaStreamSynchronize(x->stream);
-        cudaFree(xv_d); cudaFree(yv_d); cudaFree(seg_d);
+        cudaFree(xv_d); cudaFree(yv_d); cudaFree(seg_d); cudaFree(cbox_d); cudaFree(col_d);
     }
 
     DevCase& dc = x->dc;
@@ -678,9 +810,8 @@ int st_norms(st_ctx* x, double* out) {
     return ST_OK;
 }
 
-int st_skin_friction(st_ctx* x, double* cf_host, double* J) {
-    if (!x) return fail(ST_ERR_ARG, "st_skin_friction: null context");
-    // primitives + ghosts of the current state
+// wall Cf of the current state into x->cf and J into x->norm_out[7] (async)
+static int skin_friction_device(st_ctx* x) {
     const DevCase& dc = x->dc;
     if (x->nq == 5) {
         k_prim<double, 5><<<grid_for(x->ncell), 256, 0, x->stream>>>(dc, x->q, x->P);
@@ -691,14 +822,29 @@ int st_skin_friction(st_ctx* x, double* cf_host, double* J) {
     }
     const double qinf = 0.5 * x->c.rho_inf * (x->c.u_inf * x->c.u_inf + x->c.v_inf * x->c.v_inf);
     k_skin_friction<<<grid_for(x->c.ni - 1), 256, 0, x->stream>>>(dc, x->P, qinf, x->cf);
+    k_drag<<<1, 256, 0, x->stream>>>(x->cf, x->wall_dx_d, x->c.ni - 1, x->norm_out + 7);
     ST_LAUNCH_CHECK("skin friction");
-    std::vector<double> cf(x->c.ni - 1);
-    ST_CUDA(cudaMemcpyAsync(cf.data(), x->cf, cf.size() * 8, cudaMemcpyDeviceToHost, x->stream));
-    ST_CUDA(cudaStreamSynchronize(x->stream));
+    return ST_OK;
+}
+
+int st_skin_friction(st_ctx* x, double* cf_host, double* J) {
+    if (!x) return fail(ST_ERR_ARG, "st_skin_friction: null context");
+    int rc = skin_friction_device(x);
+    if (rc) return rc;
+    if (cf_host) ST_CUDA(cudaMemcpyAsync(cf_host, x->cf, (size_t)(x->c.ni - 1) * 8, cudaMemcpyDeviceToHost, x->stream));
     double s = 0.0;
-    for (size_t i = 0; i < cf.size(); i++) s += cf[i] * x->wall_dx[i];
-    if (cf_host) std::memcpy(cf_host, cf.data(), cf.size() * 8);
+    ST_CUDA(cudaMemcpyAsync(&s, x->norm_out + 7, 8, cudaMemcpyDeviceToHost, x->stream));
+    ST_CUDA(cudaStreamSynchronize(x->stream));
     if (J) *J = s;
+    return ST_OK;
+}
+
+int st_skin_friction_device(st_ctx* x, double* cf_dev, double* J_dev) {
+    if (!x) return fail(ST_ERR_ARG, "st_skin_friction_device: null context");
+    int rc = skin_friction_device(x);
+    if (rc) return rc;
+    if (cf_dev) ST_CUDA(cudaMemcpyAsync(cf_dev, x->cf, (size_t)(x->c.ni - 1) * 8, cudaMemcpyDeviceToDevice, x->stream));
+    if (J_dev) ST_CUDA(cudaMemcpyAsync(J_dev, x->norm_out + 7, 8, cudaMemcpyDeviceToDevice, x->stream));
     return ST_OK;
 }
 
@@ -794,6 +940,14 @@ int st_profile_pipeline(st_ctx* x, int which, int lhs, double* ms, int max_n, ch
         names[names_len - 1] = 0;
     }
     *n = cnt;
+    return ST_OK;
+}
+
+int st_set_residual_path(st_ctx* x, int path, int* active) {
+    if (!x || (path != 0 && path != 1)) return fail(ST_ERR_ARG, "st_set_residual_path: path must be 0 or 1");
+    if (path == 1 && !x->tile_ok) return fail(ST_ERR_UNSUPPORTED, "st_set_residual_path: tiled sweeps unavailable");
+    x->res_path = path;
+    if (active) *active = (x->tile_ok && x->res_path == 1) ? 1 : 0;
     return ST_OK;
 }
 

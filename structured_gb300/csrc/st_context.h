@@ -1,5 +1,6 @@
 // Host-side context shared by the C-ABI translation units.
 #pragma once
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <string>
@@ -74,6 +75,12 @@ struct st_ctx {
     bool jac1_is_jac = false;
     double *psi_tmp = nullptr, *outq_tmp = nullptr, *outb_tmp = nullptr, *tape = nullptr;
 
+    // tiled residual sweeps (st_tile.cuh): TMA descriptors of the primitive
+    // array P for the i- and j-sweep boxes; res_path 1 = tiled sweeps (when
+    // tile_ok), 0 = per-face passes
+    CUtensorMap tmap_i{}, tmap_j{};
+    bool tile_ok = false;
+    int res_path = 1;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     // per-launch profiling (st_profile_pipeline): an event after each launch
     bool prof_on = false;
@@ -111,8 +118,12 @@ inline void mark(st_ctx* x, const char* name) {
     x->prof_name[x->prof_n + 1] = name;
     x->prof_n++;
 }
-// forward pipeline on (q -> rhs) for the double path; beta may be null
+// forward pipeline on (q -> rhs) for the double path; beta may be null.  Runs
+// the tiled sweeps when selected and possible; run_residual_faces always runs
+// the per-face passes, which also leave the face fluxes and gradient parts in
+// Fi/Fj/Gi/Gj for callers that read them.
 int run_residual(st_ctx* ctx, const double* q, const double* beta, double* rhs, int order);
+int run_residual_faces(st_ctx* ctx, const double* q, const double* beta, double* rhs, int order);
 // forward-mode JVP of the order-`order` residual at the context state (async);
 // freeze_nonlocal holds the periodic and wake ghosts' tangents at zero (the
 // Jacobian's local part)

@@ -382,6 +382,79 @@ __device__ inline FaceIdx face_idx(const DevCase& c, int a, int b) {
 //     Writes the net flux F = F_conv - F_visc and, with SA, the gradient parts
 //     the cell source needs.
 // ----------------------------------------------------------------------------
+// The net flux of one face from its six primitive records (L, R and the side
+// pairs P, M that close the Green-Gauss dual cell) and the MUSCL slopes of L
+// (its high-face slope sL) and R (its low-face slope sR), each null on a
+// first-order side.  f[NQ]: F_conv - F_visc; with SA and viscosity g[4]
+// receives the gradient parts (u_y, v_x, nut_x, nut_y) of the cell source.
+// Shared by the per-face passes and the tiled sweeps (same arithmetic).
+template <class T, int NQ>
+__device__ __forceinline__ void face_flux(const DevCase& c, const double* __restrict__ gm, const T* pL, const T* pR,
+                                          const T* pPa, const T* pPb, const T* pMa, const T* pMb, const T* sL,
+                                          const T* sR, T* f, T* g) {
+    const int slot[5] = {P_RHO, P_U, P_V, P_P, P_NUT};
+    T qL[5], qR[5];
+#pragma unroll
+    for (int k = 0; k < NQ; k++) {
+        const int m = slot[k];
+        qL[k] = pL[m];
+        qR[k] = pR[m];
+        if (sL) qL[k] = qL[k] + sL[k];
+        if (sR) qR[k] = qR[k] - sR[k];
+    }
+    if (c.flux == ST_FLUX_AUSM)
+        ausm_flux(qL[0], qL[1], qL[2], qL[3], qR[0], qR[1], qR[2], qR[3], gm[G_NX], gm[G_NY], 2.0 * gm[G_AJ], f);
+    else
+        roe_flux(qL[0], qL[1], qL[2], qL[3], qR[0], qR[1], qR[2], qR[3], gm[G_R1], gm[G_R2], gm[G_AJ], f);
+    if (NQ == 5) f[4] = f[0] * (val(f[0]) >= 0.0 ? qL[4] : qR[4]);
+    if (c.viscous) {
+        const double wLx = gm[G_WLX], wLy = gm[G_WLY], wRx = gm[G_WRX], wRy = gm[G_WRY];
+        const double wPx = gm[G_WPX], wPy = gm[G_WPY], wMx = gm[G_WMX], wMy = gm[G_WMY];
+        // gradient and face average of one slot
+#define ST_GRAD(m, gx, gy, avg)                                                              \
+        {                                                                                    \
+            const T sP = pPa[m] + pPb[m], sM = pMa[m] + pMb[m];                              \
+            gx = wLx * pL[m] + wRx * pR[m] + wPx * sP + wMx * sM;                            \
+            gy = wLy * pL[m] + wRy * pR[m] + wPy * sP + wMy * sM;                            \
+            avg = 0.375 * (pL[m] + pR[m]) + 0.0625 * (sP + sM);                              \
+        }
+        T dudx, dudy, ubar, dvdx, dvdy, vbar, dTdx, dTdy, Tbar;
+        ST_GRAD(P_U, dudx, dudy, ubar)
+        ST_GRAD(P_V, dvdx, dvdy, vbar)
+        ST_GRAD(P_T, dTdx, dTdy, Tbar)
+        (void)Tbar;
+        const T mub = 0.375 * (pL[P_MU] + pR[P_MU]) + 0.0625 * (pPa[P_MU] + pPb[P_MU] + pMa[P_MU] + pMb[P_MU]);
+        T mu = mub, k;
+        if (NQ == 5) {
+            const T mutb = 0.375 * (pL[P_MUT] + pR[P_MUT]) + 0.0625 * (pPa[P_MUT] + pPb[P_MUT] + pMa[P_MUT] + pMb[P_MUT]);
+            mu = mub + mutb;
+            k = mub * c.cp_pr + mutb * c.cp_prt;
+        } else {
+            k = mub * c.cp_pr;
+        }
+        const double nx = gm[G_NX], ny = gm[G_NY];
+        const T tau_xy = mu * (dudy + dvdx);
+        const T tau_xx = mu * (2.0 * dudx - 2.0 / 3.0 * (dudx + dvdy));
+        const T tau_yy = mu * (2.0 * dvdy - 2.0 / 3.0 * (dudx + dvdy));
+        const T q_x = -k * dTdx;
+        const T q_y = -k * dTdy;
+        f[1] = f[1] - (tau_xx * nx + tau_xy * ny);
+        f[2] = f[2] - (tau_xy * nx + tau_yy * ny);
+        f[3] = f[3] - ((ubar * tau_xx + vbar * tau_xy - q_x) * nx + (ubar * tau_xy + vbar * tau_yy - q_y) * ny);
+        if (NQ == 5) {
+            T dndx, dndy, nbar;
+            ST_GRAD(P_NUT, dndx, dndy, nbar)
+            (void)nbar;
+#define ST_SD(p) sa_diff(p[P_RHO], p[P_NUT], p[P_MU])
+            const T rnb = 0.375 * (ST_SD(pL) + ST_SD(pR)) + 0.0625 * (ST_SD(pPa) + ST_SD(pPb) + ST_SD(pMa) + ST_SD(pMb));
+#undef ST_SD
+            f[4] = f[4] - (1.0 / SA_SIGMA) * (mub + rnb) * (dndx * nx + dndy * ny);
+            g[0] = dudy; g[1] = dvdx; g[2] = dndx; g[3] = dndy;
+        }
+#undef ST_GRAD
+    }
+}
+
 template <class T, int NQ, int DIR, int ORDER>
 __global__ void __launch_bounds__(256) k_face(DevCase c, const T* __restrict__ P, const T* __restrict__ lim,
                                               T* __restrict__ F, T* __restrict__ G) {
@@ -389,78 +462,18 @@ __global__ void __launch_bounds__(256) k_face(DevCase c, const T* __restrict__ P
     const int nb = DIR == 0 ? c.njc : c.nj;
     const size_t n = (size_t)na * nb;
     const double* geo = DIR == 0 ? c.geo_i : c.geo_j;
-    const int slot[5] = {P_RHO, P_U, P_V, P_P, P_NUT};
     for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += (size_t)gridDim.x * blockDim.x) {
         const int a = (int)(idx / nb), b = (int)(idx % nb);
         const FaceIdx fi = face_idx<DIR>(c, a, b);
-        const double* gm = geo + fi.face * NGEO;
-        const T* pL = P + fi.L;
-        const T* pR = P + fi.R;
-        T qL[5], qR[5];
+        const T* sL = (ORDER == 2 && fi.limL) ? lim + lim_off(c, DIR, LIM_SL, fi.phL) : nullptr;
+        const T* sR = (ORDER == 2 && fi.limR) ? lim + lim_off(c, DIR, LIM_SR, fi.phR) : nullptr;
+        T f[NQ], g[4];
+        face_flux<T, NQ>(c, geo + fi.face * NGEO, P + fi.L, P + fi.R, P + fi.Pa, P + fi.Pb, P + fi.Ma, P + fi.Mb, sL,
+                         sR, f, g);
+        if (NQ == 5 && c.viscous) {
+            T* go = G + fi.face * 4;
 #pragma unroll
-        for (int k = 0; k < NQ; k++) {
-            const int m = slot[k];
-            qL[k] = pL[m];
-            qR[k] = pR[m];
-            if (ORDER == 2) {
-                if (fi.limL) qL[k] = qL[k] + lim[lim_off(c, DIR, LIM_SL, fi.phL) + k];
-                if (fi.limR) qR[k] = qR[k] - lim[lim_off(c, DIR, LIM_SR, fi.phR) + k];
-            }
-        }
-        T f[NQ];
-        if (c.flux == ST_FLUX_AUSM)
-            ausm_flux(qL[0], qL[1], qL[2], qL[3], qR[0], qR[1], qR[2], qR[3], gm[G_NX], gm[G_NY], 2.0 * gm[G_AJ], f);
-        else
-            roe_flux(qL[0], qL[1], qL[2], qL[3], qR[0], qR[1], qR[2], qR[3], gm[G_R1], gm[G_R2], gm[G_AJ], f);
-        if (NQ == 5) f[4] = f[0] * (val(f[0]) >= 0.0 ? qL[4] : qR[4]);
-        if (c.viscous) {
-            const T* pPa = P + fi.Pa; const T* pPb = P + fi.Pb;
-            const T* pMa = P + fi.Ma; const T* pMb = P + fi.Mb;
-            const double wLx = gm[G_WLX], wLy = gm[G_WLY], wRx = gm[G_WRX], wRy = gm[G_WRY];
-            const double wPx = gm[G_WPX], wPy = gm[G_WPY], wMx = gm[G_WMX], wMy = gm[G_WMY];
-            // gradient and face average of one slot
-#define ST_GRAD(m, gx, gy, avg)                                                              \
-            {                                                                                \
-                const T sP = pPa[m] + pPb[m], sM = pMa[m] + pMb[m];                          \
-                gx = wLx * pL[m] + wRx * pR[m] + wPx * sP + wMx * sM;                        \
-                gy = wLy * pL[m] + wRy * pR[m] + wPy * sP + wMy * sM;                        \
-                avg = 0.375 * (pL[m] + pR[m]) + 0.0625 * (sP + sM);                          \
-            }
-            T dudx, dudy, ubar, dvdx, dvdy, vbar, dTdx, dTdy, Tbar;
-            ST_GRAD(P_U, dudx, dudy, ubar)
-            ST_GRAD(P_V, dvdx, dvdy, vbar)
-            ST_GRAD(P_T, dTdx, dTdy, Tbar)
-            (void)Tbar;
-            const T mub = 0.375 * (pL[P_MU] + pR[P_MU]) + 0.0625 * (pPa[P_MU] + pPb[P_MU] + pMa[P_MU] + pMb[P_MU]);
-            T mu = mub, k;
-            if (NQ == 5) {
-                const T mutb = 0.375 * (pL[P_MUT] + pR[P_MUT]) + 0.0625 * (pPa[P_MUT] + pPb[P_MUT] + pMa[P_MUT] + pMb[P_MUT]);
-                mu = mub + mutb;
-                k = mub * c.cp_pr + mutb * c.cp_prt;
-            } else {
-                k = mub * c.cp_pr;
-            }
-            const double nx = gm[G_NX], ny = gm[G_NY];
-            const T tau_xy = mu * (dudy + dvdx);
-            const T tau_xx = mu * (2.0 * dudx - 2.0 / 3.0 * (dudx + dvdy));
-            const T tau_yy = mu * (2.0 * dvdy - 2.0 / 3.0 * (dudx + dvdy));
-            const T q_x = -k * dTdx;
-            const T q_y = -k * dTdy;
-            f[1] = f[1] - (tau_xx * nx + tau_xy * ny);
-            f[2] = f[2] - (tau_xy * nx + tau_yy * ny);
-            f[3] = f[3] - ((ubar * tau_xx + vbar * tau_xy - q_x) * nx + (ubar * tau_xy + vbar * tau_yy - q_y) * ny);
-            if (NQ == 5) {
-                T dndx, dndy, nbar;
-                ST_GRAD(P_NUT, dndx, dndy, nbar)
-                (void)nbar;
-#define ST_SD(p) sa_diff(p[P_RHO], p[P_NUT], p[P_MU])
-                const T rnb = 0.375 * (ST_SD(pL) + ST_SD(pR)) + 0.0625 * (ST_SD(pPa) + ST_SD(pPb) + ST_SD(pMa) + ST_SD(pMb));
-#undef ST_SD
-                f[4] = f[4] - (1.0 / SA_SIGMA) * (mub + rnb) * (dndx * nx + dndy * ny);
-                T* g = G + fi.face * 4;
-                g[0] = dudy; g[1] = dvdx; g[2] = dndx; g[3] = dndy;
-            }
-#undef ST_GRAD
+            for (int t = 0; t < 4; t++) go[t] = g[t];
         }
         T* o = F + fi.face * NQ;
 #pragma unroll

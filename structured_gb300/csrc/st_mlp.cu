@@ -451,7 +451,7 @@ int st_mlp_grad(st_ctx* x, const float* feat_dev, const float* target_dev, long 
 int st_sa_features(st_ctx* x, float* feat_dev) {
     if (!x || !feat_dev) return fail(ST_ERR_ARG, "st_sa_features: null argument");
     if (x->nq != 5 || !x->dc.viscous) return fail(ST_ERR_UNSUPPORTED, "st_sa_features: needs the viscous SA model");
-    int rc = stx::run_residual(x, x->q, x->beta, x->rhs, x->c.order);
+    int rc = stx::run_residual_faces(x, x->q, x->beta, x->rhs, x->c.order);
     if (rc) return rc;
     k_sa_features<<<grid_for(x->ncell), 256, 0, x->stream>>>(x->dc, x->P, x->Gj, feat_dev);
     ST_LAUNCH_CHECK("features");
@@ -463,7 +463,7 @@ int st_mlp_beta(st_ctx* x, double* beta_dev) {
     if (!x || !beta_dev) return fail(ST_ERR_ARG, "st_mlp_beta: null argument");
     if (!x->mlp_wb) return fail(ST_ERR_ARG, "st_mlp_beta: no network");
     if (x->nq != 5 || !x->dc.viscous) return fail(ST_ERR_UNSUPPORTED, "st_mlp_beta: needs the viscous SA model");
-    int rc = stx::run_residual(x, x->q, x->beta, x->rhs, x->c.order);
+    int rc = stx::run_residual_faces(x, x->q, x->beta, x->rhs, x->c.order);
     if (rc) return rc;
     DevCase dc = x->dc;
     dc.mlp_wb = x->mlp_wb;

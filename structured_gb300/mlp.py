@@ -33,10 +33,28 @@ def _case_of(path: str):
     return tag, workloads.turbulent_plate(tempfile.mkdtemp(), ni, nj, re_l, ang, write_files=False)
 
 
+class _Case:
+    """An inversion file's arrays, with the grid (regenerated from the case
+    when the file does not hold it) and the inverted state in FP64."""
+
+    def __init__(self, path, c):
+        from . import case as C
+        self._d = dict(np.load(path))
+        if "xv" not in self._d:
+            m = re.search(r"_a([+-][0-9]+)_", os.path.basename(path))
+            g = C.flat_plate_grid(c.ni, c.nj, h1=1e-7, ratio=1.05, top_angle_deg=float(m.group(1)))
+            self._d["xv"], self._d["yv"] = g.xv, g.yv
+        self._d["q_inv"] = np.ascontiguousarray(self._d["q_inv"], dtype=np.float64)
+        self.files = list(self._d)
+
+    def __getitem__(self, k):
+        return self._d[k]
+
+
 def _eq_for(path: str):
     from .solver import EulerEquation
     tag, c = _case_of(path)
-    d = np.load(path)
+    d = _Case(path, c)
     return tag, c, d, EulerEquation(c, d["xv"], d["yv"])
 
 
@@ -63,12 +81,20 @@ def cf_error(cf, cf_ref, mask):
 def inversion_cf_error(path: str) -> float:
     from . import inversion as inv
     _, c = _case_of(path)
-    d = np.load(path)
+    d = _Case(path, c)
     return cf_error(d["cf_inv"], d["cf_target"], inv.plate_mask(c, d["xv"]))
 
 
+def _re_of(path: str) -> str:
+    return re.search(r"inversion_(Re[0-9.e+]+)_", os.path.basename(path)).group(1)
+
+
 def run(data_dir: str, steps: int = 2000, batch: int = 65536, lr: float = 1e-3, seed: int = 20261203,
-        max_cf_err: float = 0.05, log=print):
+        max_cf_err: float = 0.05, train_mode: str = "all", log=print):
+    """train_mode: "all" (every other case whose inversion matched its target
+    within max_cf_err), "same_re" (those of them at the held-out case's
+    Reynolds number) or "self" (the held-out case's own inversion: the
+    feature set's upper bound, not a generalisation result)."""
     import torch
     from . import inversion as inv
     paths = sorted(glob.glob(os.path.join(data_dir, "inversion_*.npz")))
@@ -76,9 +102,14 @@ def run(data_dir: str, steps: int = 2000, batch: int = 65536, lr: float = 1e-3, 
     others = [p for p in paths if HELD_OUT not in os.path.basename(p)]
     errs = {os.path.basename(p): inversion_cf_error(p) for p in others}
     train_paths = [p for p in others if errs[os.path.basename(p)] <= max_cf_err]
+    if train_mode == "same_re" and test_paths:
+        train_paths = [p for p in train_paths if _re_of(p) == _re_of(test_paths[0])]
+    elif train_mode == "self":
+        train_paths = list(test_paths)
     if not train_paths or not test_paths:
         raise FileNotFoundError("need the held-out case %s and training cases in %s" % (HELD_OUT, data_dir))
-    out = {"train_cases": [os.path.basename(p) for p in train_paths], "held_out": os.path.basename(test_paths[0]),
+    out = {"train_mode": train_mode, "train_cases": [os.path.basename(p) for p in train_paths],
+           "held_out": os.path.basename(test_paths[0]),
            "excluded": {k: v for k, v in errs.items() if v > max_cf_err}}
     t0 = time.time()
     feat, target = training_set(train_paths)
@@ -136,6 +167,14 @@ def run(data_dir: str, steps: int = 2000, batch: int = 65536, lr: float = 1e-3, 
         log("[%s] %s" % (label, res))
         return res, cf
 
+    if "inversion_wall_s" in d.files:
+        # the held-out case's own field inversion: total wall time, and the
+        # time to its first iterate whose Cf is within 1 % of its final Cf
+        tw = d["iter_wall_s"]
+        within = [float(t) for t, cf in zip(tw, d["iter_cf"]) if cf_error(cf, cf_inv, mask) <= 0.01]
+        out["field_inversion"] = {"wall_s": float(d["inversion_wall_s"]),
+                                  "wall_s_to_cf_err_1pct": within[0] if within else float(d["inversion_wall_s"]),
+                                  "iterations": int(len(tw) - 1)}
     out["plain_sa"], _ = solve("plain SA")
     out["inverted_beta"], _ = solve("inverted beta", beta=d["beta_inv"])
     out["learned"], cf_l = solve("learned", learned=True)

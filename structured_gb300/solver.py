@@ -70,6 +70,7 @@ def load_library() -> ctypes.CDLL:
         "st_dt": (I, [V, D, _P]),
         "st_norms": (I, [V, _P]),
         "st_skin_friction": (I, [V, _P, ctypes.POINTER(D)]),
+        "st_skin_friction_device": (I, [V, V, V]),
         "st_jvp_device": (I, [V, V, V, V, I]),
         "st_vjp_device": (I, [V, V, V, V, I]),
         "st_vjp": (I, [V, _P, _P, _P, I]),
@@ -77,6 +78,7 @@ def load_library() -> ctypes.CDLL:
         "st_residual_vjp": (I, [V, _P, _P, _P, _P, I]),
         "st_fused_launch_count": (I, [V, I]),
         "st_probe_fp64": (I, [V, ctypes.POINTER(D)]),
+        "st_set_residual_path": (I, [V, I, ctypes.POINTER(I)]),
         "st_probe_nr_math": (I, [V, ctypes.c_longlong, V]),
         "st_last_kernel_ms": (I, [V, ctypes.POINTER(D), ctypes.POINTER(D)]),
         "st_profile_pipeline": (I, [V, I, I, _P, I, ctypes.c_char_p, I, ctypes.POINTER(I)]),
@@ -245,6 +247,13 @@ class EulerEquation:
         q, r, s = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
         _check(self.lib.st_device_state(self.h, ctypes.byref(q), ctypes.byref(r), ctypes.byref(s)), "st_device_state")
         return q.value, r.value, s.value
+
+    def set_residual_path(self, tiled: bool) -> bool:
+        """Selects the tiled (TMA-staged) sweeps or the per-stage passes for
+        the FP64 residual; returns whether the tiled sweeps now run."""
+        act = ctypes.c_int()
+        _check(self.lib.st_set_residual_path(self.h, int(tiled), ctypes.byref(act)), "st_set_residual_path")
+        return bool(act.value)
 
     def probe_fp64_tflops(self) -> float:
         t = ctypes.c_double()

@@ -156,7 +156,14 @@ def inversions(ni: int, nj: int, iters: int, out_dir: str | None, only: str | No
             log("[case] " + json.dumps(summary))
             if out_dir:
                 os.makedirs(out_dir, exist_ok=True)
-                np.savez_compressed(os.path.join(out_dir, "inversion_%s_%dx%d.npz" % (tag, ni, nj)), **arrays)
+                # what training and the held-out comparison read: the inverted
+                # beta (FP64), the inverted state for the features (FP32), the
+                # wall Cf arrays and the inversion's history; the grid is
+                # regenerated from the case
+                keep = {k: arrays[k] for k in ("beta_inv", "cf_target", "cf_inv", "cf_base", "iter_wall_s", "iter_cf",
+                                               "inversion_wall_s")}
+                keep["q_inv"] = arrays["q_inv"].astype(np.float32)
+                np.savez_compressed(os.path.join(out_dir, "inversion_%s_%dx%d.npz" % (tag, ni, nj)), **keep)
                 with open(os.path.join(out_dir, "inversions_%dx%d.json" % (ni, nj)), "w") as f:
                     json.dump(summaries, f, indent=1)
     return summaries
@@ -174,13 +181,14 @@ def main(argv=None):
     ap.add_argument("--nj", type=int, default=385)
     ap.add_argument("--tangent", type=int, default=8)
     ap.add_argument("--out", default=None)
+    ap.add_argument("--train", default="all", choices=["all", "same_re", "self"])
     a = ap.parse_args(argv)
     if a.what == "inversion":
         inversions(a.ni, a.nj, a.iters, a.out, a.only, log=lambda m: print(m, flush=True))
         return 0
     if a.what == "mlp":
         from . import mlp
-        res, params, loss = mlp.run(a.data, steps=a.steps, log=lambda m: print(m, flush=True))
+        res, params, loss = mlp.run(a.data, steps=a.steps, train_mode=a.train, log=lambda m: print(m, flush=True))
         print(json.dumps(res, indent=1))
         if a.out:
             with open(a.out, "w") as f:
