@@ -134,10 +134,11 @@ int st_residual_device(st_ctx* ctx, const double* q_dev, const double* beta_dev,
                        double* rhs_dev, int lhs);
 
 /* Which kernels evaluate the FP64 residual of st_residual*, the Newton and
- * explicit solvers: path 1 (the default where available) = tiled i- and
- * j-sweeps whose CTAs stage their tile of primitive records plus a two-cell
- * halo in shared memory by TMA and keep slopes and face fluxes on chip;
- * path 0 = one pass per stage (slopes, i-faces, j-faces, cells) through HBM.
+ * explicit solvers: path 1 = tiled i- and j-sweeps whose CTAs stage their
+ * tile of primitive records plus a two-cell halo in shared memory by TMA and
+ * keep slopes and face fluxes on chip; path 0 (the default) = one pass per
+ * stage (slopes, i-faces, j-faces, cells) through HBM, measured faster on
+ * this FP64-issue-bound residual.
  * Both compute the stages of calc_residual (eulerequation.cpp:168-232) with
  * the same face arithmetic.  The network-beta residual and JVPs always use the
  * per-stage passes.  *active (may be NULL) = 1 if the tiled sweeps now run.

@@ -28,7 +28,7 @@ def nvcc() -> str:
 
 def flags(verbose_ptxas: bool = False) -> list:
     f = ARCH + ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr",
-                "-Xcompiler", "-fPIC,-ffp-contract=off,-O2", "-I", os.path.join(HERE, "..", "include")]
+                "-Xcompiler", "-fPIC,-ffp-contract=off,-O2,-fopenmp", "-I", os.path.join(HERE, "..", "include")]
     if verbose_ptxas:
         f += ["-Xptxas", "-v"]
     return f
@@ -58,7 +58,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
             if rc:
                 raise RuntimeError("nvcc failed on %s" % src)
             objs.append(obj)
-    cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"]
+    cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart", "-lgomp"]
     p = subprocess.run(cmd, capture_output=True, text=True)
     if p.returncode:
         sys.stderr.write(p.stdout + p.stderr)

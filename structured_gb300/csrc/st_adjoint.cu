@@ -45,7 +45,16 @@ int launch_fused(st_ctx* x, const double* psi, double* rhs, double* outq, double
     const unsigned gc = grid_for(x->ncell);
     k_prim<double, NQ><<<gc, 256, 0, s>>>(dc, x->q, x->P);
     stx::mark(x, "k_prim");
-    k_bc_taped<NQ><<<1, 1024, 0, s>>>(dc, x->P, x->tape);
+    {  // boundary pass with the ghost ring recorded before each BC, as grid-wide launches
+        const unsigned gr = (unsigned)((2 * (x->c.ni + 1) + 2 * (x->c.nj - 1) + 255) / 256);
+        const unsigned gb = (unsigned)((std::max(x->c.ni, x->c.nj) + 1 + 255) / 256);
+        for (int b = 0; b < (int)x->bcs.size(); b++) {
+            k_tape_ring<<<gr, 256, 0, s>>>(dc, x->P, x->tape, b);
+            k_bc_one<double, NQ><<<gb, 256, 0, s>>>(dc, x->P, b, 0);
+            if (x->bcs[b].type == ST_BC_WAKE) k_bc_one<double, NQ><<<gb, 256, 0, s>>>(dc, x->P, b, 1);
+        }
+        if (dc.viscous) k_bc_mu<double, NQ><<<gr, 256, 0, s>>>(dc, x->P);
+    }
     stx::mark(x, "k_bc_taped");
     if (ORDER == 2) {
         k_limiter<double, NQ, true><<<gc, 256, 0, s>>>(dc, x->P, x->lim);
@@ -70,7 +79,15 @@ int launch_fused(st_ctx* x, const double* psi, double* rhs, double* outq, double
     }
     k_gather<NQ, ORDER><<<grid_for(x->npad), 256, 0, s>>>(dc, x->P, x->arec_i, x->arec_j, x->srec, x->Pbar);
     stx::mark(x, "k_gather");
-    k_bc_adj<NQ><<<1, 1024, 0, s>>>(dc, x->P, x->tape, x->Pbar);
+    {
+        const unsigned gr = (unsigned)((2 * (x->c.ni + 1) + 2 * (x->c.nj - 1) + 255) / 256);
+        const unsigned gb = (unsigned)((std::max(x->c.ni, x->c.nj) + 1 + 255) / 256);
+        if (dc.viscous) k_bc_adj_mu<NQ><<<gr, 256, 0, s>>>(dc, x->P, x->Pbar);
+        for (int b = (int)x->bcs.size() - 1; b >= 0; b--) {
+            k_bc_adj_one<NQ><<<gb, 256, 0, s>>>(dc, x->P, x->tape, x->Pbar, b, 0);
+            if (x->bcs[b].type == ST_BC_WAKE) k_bc_adj_one<NQ><<<gb, 256, 0, s>>>(dc, x->P, x->tape, x->Pbar, b, 1);
+        }
+    }
     stx::mark(x, "k_bc_adj");
     k_prim_adj<NQ><<<gc, 256, 0, s>>>(dc, x->q, x->P, x->Pbar, outq);
     stx::mark(x, "k_prim_adj");
@@ -78,8 +95,18 @@ int launch_fused(st_ctx* x, const double* psi, double* rhs, double* outq, double
     return ST_OK;
 }
 
+// launches of the grid-wide boundary pass: one per BC (two for a wake cut),
+// plus the ghost viscosities when viscous
+int bc_launches(const st_ctx* x) {
+    int n = 0;
+    for (const auto& b : x->bcs) n += b.type == ST_BC_WAKE ? 2 : 1;
+    return n + (x->dc.viscous ? 1 : 0);
+}
+
 int fused_launches(const st_ctx* x, int order, bool with_rhs) {
-    int n = 7;  // prim, bc, face x2, gather, bc_adj, prim_adj
+    int n = 5;  // prim, face x2, gather, prim_adj
+    n += bc_launches(x) + (int)x->bcs.size();  // taped boundary pass: a ring copy before each BC
+    n += bc_launches(x);                        // its reverse
     if (order == 2) n += 1;
     if (x->nq == 5 && x->dc.viscous) n += 3;
     if (with_rhs) n += 1;
@@ -161,7 +188,11 @@ int st_residual_vjp(st_ctx* x, const double* psi_host, double* rhs_host, double*
 int st_launch_counts(st_ctx* x, int lhs, int* residual, int* vjp) {
     if (!x) return fail(ST_ERR_ARG, "st_launch_counts: null context");
     const int order = lhs ? x->c.lhs_order : x->c.order;
-    if (residual) *residual = order == 2 ? 6 : 5;
+    if (residual) {
+        // prim, the boundary pass, then the two tiled sweeps or the per-stage passes
+        const bool tiled = x->tile_ok && x->res_path == 1 && !x->dc.mlp_wb;
+        *residual = 1 + bc_launches(x) + (tiled ? 2 : (order == 2 ? 4 : 3));
+    }
     if (vjp) *vjp = fused_launches(x, order, false);
     return ST_OK;
 }

@@ -690,20 +690,20 @@ __global__ void __launch_bounds__(1024) k_bc_taped(DevCase c, double* __restrict
         bc_apply_block<double, NQ>(one, P);
         __syncthreads();
     }
-    if (c.viscous) bc_ghost_mu<double, NQ>(c, P);
+    if (c.viscous) bc_ghost_mu<double, NQ>(c, P, threadIdx.x, blockDim.x);
 }
 
-// R5: reverse of the boundary pass.  First the ghost mu, mu_t, then each BC in
-// reverse order: the ghost adjoint flows to the BC's inputs (read from the
-// tape where they are ghosts themselves) and is cleared.
+// R5: reverse of the boundary pass.  First the ghost mu, mu_t (bc_adj_mu),
+// then each BC in reverse order (bc_adj_one): the ghost adjoint flows to the
+// BC's inputs (read from the tape where they are ghosts themselves) and is
+// cleared.  A wake cut is reversed in two parts, its second ghost half first.
+// Threads tid = 0 .. nth-1 of a block or of a launch.
 template <int NQ>
-__global__ void __launch_bounds__(1024) k_bc_adj(DevCase c, const double* __restrict__ P, const double* __restrict__ tape,
-                                                 double* __restrict__ Pbar) {
+__device__ void bc_adj_mu(const DevCase& c, const double* __restrict__ P, double* __restrict__ Pbar, int tid, int nth) {
     const int nic = c.nic, njc = c.njc;
     const int nr = ring_size(c);
-    const double iR = c.iR;
-    if (c.viscous) {
-        for (int r = threadIdx.x; r < nr; r += blockDim.x) {
+    {
+        for (int r = tid; r < nr; r += nth) {
             int ip, jp;
             if (r < nic + 2) { ip = r; jp = 0; }
             else if (r < 2 * (nic + 2)) { ip = r - (nic + 2); jp = njc + 1; }
@@ -731,27 +731,35 @@ __global__ void __launch_bounds__(1024) k_bc_adj(DevCase c, const double* __rest
             gb[P_MU] = 0.0;
             gb[P_MUT] = 0.0;
         }
-        __syncthreads();
     }
+}
+
+template <int NQ>
+__device__ void bc_adj_one(const DevCase& c, const double* __restrict__ P, const double* __restrict__ tape,
+                           double* __restrict__ Pbar, int b, int part, int tid, int nth) {
+    const int nic = c.nic, njc = c.njc;
+    const int nr = ring_size(c);
+    const double iR = c.iR;
     // input value: ghost inputs from the tape before BC b, interior from P
     auto in = [&](int b, int ip, int jp, int s) -> double {
         if (on_ring(c, ip, jp)) return tape[((size_t)b * nr + ring_index(c, ip, jp)) * RW + s];
         return P[pidx(c, ip, jp) + s];
     };
-    for (int b = c.nbc - 1; b >= 0; b--) {
+    {
         const DevBC bc = c.bcs[b];
         const bool bt = (bc.face == 0 || bc.face == 2);
         const int end = bc.end >= 0 ? bc.end : (bt ? nic : njc) + 2 + bc.end;
         const int start = bc.start;
+        if (part == 1 && bc.type != 6) return;
         if (bc.type == 0) {
-            for (int s = start + threadIdx.x; s <= end; s += blockDim.x) {
+            for (int s = start + tid; s <= end; s += nth) {
                 int ip = bt ? s : (bc.face == 3 ? 0 : nic + 1);
                 int jp = bt ? (bc.face == 0 ? 0 : njc + 1) : s;
                 double* gb = Pbar + pidx(c, ip, jp);
                 for (int t = 0; t < RW; t++) gb[t] = 0.0;
             }
         } else if (bc.type == 1 && bt) {
-            for (int ip = start + threadIdx.x; ip <= end; ip += blockDim.x) {
+            for (int ip = start + tid; ip <= end; ip += nth) {
                 const bool bot = (bc.face == 0);
                 const int jg = bot ? 0 : njc + 1, j1 = bot ? 1 : njc, j2 = bot ? 2 : njc - 1;
                 const double* nn = c.neta + ((size_t)(ip - 1) * c.nj + (bot ? 0 : njc)) * 2;
@@ -772,7 +780,7 @@ __global__ void __launch_bounds__(1024) k_bc_adj(DevCase c, const double* __rest
                 for (int t = 0; t < RW; t++) gb[t] = 0.0;
             }
         } else if (bc.type == 2 || bc.type == 5) {
-            for (int s = start + threadIdx.x; s <= end; s += blockDim.x) {
+            for (int s = start + tid; s <= end; s += nth) {
                 int gi, gj, ai_, aj_, di, dj;
                 if (bt) {
                     const bool bot = (bc.face == 0);
@@ -804,7 +812,7 @@ __global__ void __launch_bounds__(1024) k_bc_adj(DevCase c, const double* __rest
                 for (int t = 0; t < RW; t++) gb[t] = 0.0;
             }
         } else if (bc.type == 3 && !bt && bc.face == 1) {
-            for (int jp = start + threadIdx.x; jp <= end; jp += blockDim.x) {
+            for (int jp = start + tid; jp <= end; jp += nth) {
                 double* gb = Pbar + pidx(c, nic + 1, jp);
                 double* ab = Pbar + pidx(c, nic, jp);
                 const double rg = in(b, nic, jp, P_RHO);
@@ -813,7 +821,7 @@ __global__ void __launch_bounds__(1024) k_bc_adj(DevCase c, const double* __rest
                 for (int t = 0; t < RW; t++) gb[t] = 0.0;
             }
         } else if (bc.type == 4) {
-            for (int s = start + threadIdx.x; s <= end; s += blockDim.x) {
+            for (int s = start + tid; s <= end; s += nth) {
                 int g0i, g0j, s0i, s0j, g1i, g1j, s1i, s1j;
                 if (bt) { g0i = s; g0j = 0; s0i = s; s0j = njc; g1i = s; g1j = njc + 1; s1i = s; s1j = 1; }
                 else { g0i = 0; g0j = s; s0i = nic; s0j = s; g1i = nic + 1; g1j = s; s1i = 1; s1j = s; }
@@ -826,19 +834,61 @@ __global__ void __launch_bounds__(1024) k_bc_adj(DevCase c, const double* __rest
             }
         } else if (bc.type == 6 && bt) {
             const int jg = (bc.face == 0) ? 0 : njc + 1;
-            for (int ip = start + threadIdx.x; ip <= end; ip += blockDim.x) {
-                double* gb = Pbar + pidx(c, nic + 1 - ip, jg);
-                double* sb = Pbar + pidx(c, ip, 1);
-                for (int t = 0; t < RW; t++) { sb[t] += gb[t]; gb[t] = 0.0; }
-            }
-            __syncthreads();
-            for (int ip = start + threadIdx.x; ip <= end; ip += blockDim.x) {
-                double* gb = Pbar + pidx(c, ip, jg);
-                double* sb = Pbar + pidx(c, nic + 1 - ip, 1);
-                for (int t = 0; t < RW; t++) { sb[t] += gb[t]; gb[t] = 0.0; }
-            }
+            if (part == 0)
+                for (int ip = start + tid; ip <= end; ip += nth) {
+                    double* gb = Pbar + pidx(c, nic + 1 - ip, jg);
+                    double* sb = Pbar + pidx(c, ip, 1);
+                    for (int t = 0; t < RW; t++) { sb[t] += gb[t]; gb[t] = 0.0; }
+                }
+            else
+                for (int ip = start + tid; ip <= end; ip += nth) {
+                    double* gb = Pbar + pidx(c, ip, jg);
+                    double* sb = Pbar + pidx(c, nic + 1 - ip, 1);
+                    for (int t = 0; t < RW; t++) { sb[t] += gb[t]; gb[t] = 0.0; }
+                }
         }
+    }
+}
+
+template <int NQ>
+__global__ void __launch_bounds__(1024) k_bc_adj(DevCase c, const double* __restrict__ P, const double* __restrict__ tape,
+                                                 double* __restrict__ Pbar) {
+    if (c.viscous) {
+        bc_adj_mu<NQ>(c, P, Pbar, threadIdx.x, blockDim.x);
         __syncthreads();
+    }
+    for (int b = c.nbc - 1; b >= 0; b--)
+        for (int part = 0; part < 2; part++) {
+            bc_adj_one<NQ>(c, P, tape, Pbar, b, part, threadIdx.x, blockDim.x);
+            __syncthreads();
+        }
+}
+
+// Grid-wide launches of the same passes (one per BC and part, issued in order
+// by the host), and of the taped forward pass: the ring is recorded before
+// BC b by k_tape_ring, then BC b is applied by k_bc_one.
+template <int NQ>
+__global__ void __launch_bounds__(256) k_bc_adj_mu(DevCase c, const double* __restrict__ P, double* __restrict__ Pbar) {
+    bc_adj_mu<NQ>(c, P, Pbar, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+}
+template <int NQ>
+__global__ void __launch_bounds__(256) k_bc_adj_one(DevCase c, const double* __restrict__ P,
+                                                     const double* __restrict__ tape, double* __restrict__ Pbar, int b,
+                                                     int part) {
+    bc_adj_one<NQ>(c, P, tape, Pbar, b, part, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+}
+static __global__ void __launch_bounds__(256) k_tape_ring(DevCase c, const double* __restrict__ P, double* __restrict__ tape,
+                                                   int b) {
+    const int nr = ring_size(c);
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nr; r += gridDim.x * blockDim.x) {
+        int ip, jp;
+        if (r < c.nic + 2) { ip = r; jp = 0; }
+        else if (r < 2 * (c.nic + 2)) { ip = r - (c.nic + 2); jp = c.njc + 1; }
+        else if (r < 2 * (c.nic + 2) + c.njc) { ip = 0; jp = r - 2 * (c.nic + 2) + 1; }
+        else { ip = c.nic + 1; jp = r - 2 * (c.nic + 2) - c.njc + 1; }
+        const double* g = P + pidx(c, ip, jp);
+        double* t = tape + ((size_t)b * nr + r) * RW;
+        for (int k = 0; k < RW; k++) t[k] = g[k];
     }
 }
 

@@ -359,7 +359,7 @@ int launch_forward(st_ctx* x, const DevCase& dc, const T* q, const T* beta, T* P
     const unsigned gc = grid_for(x->ncell);
     k_prim<T, NQ><<<gc, 256, 0, s>>>(dc, q, P);
     stx::mark(x, "k_prim");
-    k_bc<T, NQ><<<1, 1024, 0, s>>>(dc, P);
+    launch_bcs<T, NQ>(dc, x->bcs.data(), (int)x->bcs.size(), P, s);
     stx::mark(x, "k_bc");
     if (order == 2) {
         k_limiter<T, NQ, false><<<gc, 256, 0, s>>>(dc, P, lim);
@@ -394,7 +394,7 @@ int launch_tiled(st_ctx* x, const double* q, const double* beta, double* rhs, in
     const int nic = x->c.ni - 1, njc = x->c.nj - 1;
     k_prim<double, NQ><<<grid_for(x->ncell), 256, 0, s>>>(dc, q, x->P);
     stx::mark(x, "k_prim");
-    k_bc<double, NQ><<<1, 1024, 0, s>>>(dc, x->P);
+    launch_bcs<double, NQ>(dc, x->bcs.data(), (int)x->bcs.size(), x->P, s);
     stx::mark(x, "k_bc");
     const dim3 gi((nic + TI_I - 1) / TI_I, (njc + TJ_I - 1) / TJ_I);
     const dim3 gj((njc + TJ_J - 1) / TJ_J, (nic + TI_J - 1) / TI_J);

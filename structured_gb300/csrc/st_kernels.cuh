@@ -58,18 +58,22 @@ __device__ inline void bc_copy_nl(const DevCase& c, T* g, const T* s) {
     }
 }
 
-// All threads of the block apply c.bcs[0..nbc) in order.
+// Boundary condition b of the list, applied by threads tid = 0 .. nth-1 of a
+// launch (or of a block).  The wake cut writes its two ghost halves in two
+// parts (part 0, then part 1 after every thread finished part 0); every other
+// type is done in part 0 and ignores part 1.
 template <class T, int NQ>
-__device__ void bc_apply_block(const DevCase& c, T* __restrict__ P) {
+__device__ void bc_apply_one(const DevCase& c, T* __restrict__ P, int b, int part, int tid, int nth) {
     const int nic = c.nic, njc = c.njc;
     const double iR = c.iR;
-    for (int b = 0; b < c.nbc; b++) {
+    {
         const DevBC bc = c.bcs[b];
         const bool bt = (bc.face == 0 || bc.face == 2);
         const int end = bc.end >= 0 ? bc.end : (bt ? nic : njc) + 2 + bc.end;
         const int start = bc.start;
+        if (part == 1 && bc.type != 6) return;
         if (bc.type == 0) {  // freestream, bc.cpp:26-60
-            for (int s = start + threadIdx.x; s <= end; s += blockDim.x) {
+            for (int s = start + tid; s <= end; s += nth) {
                 int ip = bt ? s : (bc.face == 3 ? 0 : nic + 1);
                 int jp = bt ? (bc.face == 0 ? 0 : njc + 1) : s;
                 T* g = P + pidx(c, ip, jp);
@@ -79,7 +83,7 @@ __device__ void bc_apply_block(const DevCase& c, T* __restrict__ P) {
             }
         } else if (bc.type == 1) {  // slip wall, bc.cpp:78-128
             if (bt) {
-                for (int ip = start + threadIdx.x; ip <= end; ip += blockDim.x) {
+                for (int ip = start + tid; ip <= end; ip += nth) {
                     const bool bot = (bc.face == 0);
                     const int jg = bot ? 0 : njc + 1, j1 = bot ? 1 : njc, j2 = bot ? 2 : njc - 1;
                     const double* nn = c.neta + ((size_t)(ip - 1) * c.nj + (bot ? 0 : njc)) * 2;
@@ -98,7 +102,7 @@ __device__ void bc_apply_block(const DevCase& c, T* __restrict__ P) {
                 }
             }
         } else if (bc.type == 2 || bc.type == 5) {  // adiabatic wall bc.cpp:150-204, isothermal :388-427
-            for (int s = start + threadIdx.x; s <= end; s += blockDim.x) {
+            for (int s = start + tid; s <= end; s += nth) {
                 T *g; const T *a, *d;
                 if (bt) {
                     const bool bot = (bc.face == 0);
@@ -127,7 +131,7 @@ __device__ void bc_apply_block(const DevCase& c, T* __restrict__ P) {
             }
         } else if (bc.type == 3) {  // outflow, bc.cpp:284-311 (right face)
             if (!bt && bc.face == 1) {
-                for (int jp = start + threadIdx.x; jp <= end; jp += blockDim.x) {
+                for (int jp = start + tid; jp <= end; jp += nth) {
                     T* g = P + pidx(c, nic + 1, jp);
                     const T* a = P + pidx(c, nic, jp);
                     g[P_RHO] = a[P_RHO]; g[P_U] = a[P_U]; g[P_V] = a[P_V]; g[P_P] = c.p_inf;
@@ -136,7 +140,7 @@ __device__ void bc_apply_block(const DevCase& c, T* __restrict__ P) {
                 }
             }
         } else if (bc.type == 4) {  // periodic, bc.cpp:329-365
-            for (int s = start + threadIdx.x; s <= end; s += blockDim.x) {
+            for (int s = start + tid; s <= end; s += nth) {
                 if (bt) {
                     bc_copy_nl(c, P + pidx(c, s, 0), P + pidx(c, s, njc));
                     bc_copy_nl(c, P + pidx(c, s, njc + 1), P + pidx(c, s, 1));
@@ -148,25 +152,36 @@ __device__ void bc_apply_block(const DevCase& c, T* __restrict__ P) {
         } else if (bc.type == 6) {  // wake, bc.cpp:224-263
             if (bt) {
                 const int jg = (bc.face == 0) ? 0 : njc + 1;
-                for (int ip = start + threadIdx.x; ip <= end; ip += blockDim.x)
-                    bc_copy_nl(c, P + pidx(c, ip, jg), P + pidx(c, nic + 1 - ip, 1));
-                __syncthreads();
-                for (int ip = start + threadIdx.x; ip <= end; ip += blockDim.x)
-                    bc_copy_nl(c, P + pidx(c, nic + 1 - ip, jg), P + pidx(c, ip, 1));
+                if (part == 0)
+                    for (int ip = start + tid; ip <= end; ip += nth)
+                        bc_copy_nl(c, P + pidx(c, ip, jg), P + pidx(c, nic + 1 - ip, 1));
+                else
+                    for (int ip = start + tid; ip <= end; ip += nth)
+                        bc_copy_nl(c, P + pidx(c, nic + 1 - ip, jg), P + pidx(c, ip, 1));
             }
         }
-        __syncthreads();
+    }
+}
+
+// All threads of the block apply c.bcs[0..nbc) in order.
+template <class T, int NQ>
+__device__ void bc_apply_block(const DevCase& c, T* __restrict__ P) {
+    for (int b = 0; b < c.nbc; b++) {
+        for (int part = 0; part < 2; part++) {
+            bc_apply_one<T, NQ>(c, P, b, part, threadIdx.x, blockDim.x);
+            __syncthreads();
+        }
     }
 }
 
 // mu, mu_t of every ghost cell (eulerequation.cpp:183-188 covers the whole
 // padded array)
 template <class T, int NQ>
-__device__ void bc_ghost_mu(const DevCase& c, T* __restrict__ P) {
+__device__ void bc_ghost_mu(const DevCase& c, T* __restrict__ P, int tid, int nth) {
     const int nic = c.nic, njc = c.njc;
     {
         const int nring = 2 * (nic + 2) + 2 * njc;
-        for (int r = threadIdx.x; r < nring; r += blockDim.x) {
+        for (int r = tid; r < nring; r += nth) {
             int ip, jp;
             if (r < nic + 2) { ip = r; jp = 0; }
             else if (r < 2 * (nic + 2)) { ip = r - (nic + 2); jp = njc + 1; }
@@ -183,7 +198,31 @@ __device__ void bc_ghost_mu(const DevCase& c, T* __restrict__ P) {
 template <class T, int NQ>
 __global__ void __launch_bounds__(1024) k_bc(DevCase c, T* __restrict__ P) {
     bc_apply_block<T, NQ>(c, P);
-    if (c.viscous) bc_ghost_mu<T, NQ>(c, P);
+    if (c.viscous) bc_ghost_mu<T, NQ>(c, P, threadIdx.x, blockDim.x);
+}
+
+// The same boundary pass as a sequence of grid-wide launches: one per
+// boundary condition (two for a wake cut), in list order, then the ghost
+// viscosities (bc_launches in the host code issues them).
+template <class T, int NQ>
+__global__ void __launch_bounds__(256) k_bc_one(DevCase c, T* __restrict__ P, int b, int part) {
+    bc_apply_one<T, NQ>(c, P, b, part, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+}
+template <class T, int NQ>
+__global__ void __launch_bounds__(256) k_bc_mu(DevCase c, T* __restrict__ P) {
+    bc_ghost_mu<T, NQ>(c, P, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+}
+
+// Host side: the boundary pass as grid-wide launches on stream s (bcs: the
+// host copy of the list, for the wake cut's second part).
+template <class T, int NQ>
+inline void launch_bcs(const DevCase& dc, const st_bc* bcs, int nbc, T* P, cudaStream_t s) {
+    const unsigned g = (unsigned)((max(dc.nic, dc.njc) + 2 + 255) / 256);
+    for (int b = 0; b < nbc; b++) {
+        k_bc_one<T, NQ><<<g, 256, 0, s>>>(dc, P, b, 0);
+        if (bcs[b].type == ST_BC_WAKE) k_bc_one<T, NQ><<<g, 256, 0, s>>>(dc, P, b, 1);
+    }
+    if (dc.viscous) k_bc_mu<T, NQ><<<(unsigned)((2 * (dc.nic + 2) + 2 * dc.njc + 255) / 256), 256, 0, s>>>(dc, P);
 }
 
 // ----------------------------------------------------------------------------

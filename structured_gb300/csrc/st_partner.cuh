@@ -303,14 +303,15 @@ inline int dense_invert(int n, double* A, double* inv) {
             }
         const double d = 1.0 / A[(long)c * n + c];
         for (int l = 0; l < n; l++) { A[(long)c * n + l] *= d; inv[(long)c * n + l] *= d; }
+        // columns < c of A are already zero outside their pivot rows; the rows
+        // are independent here, so the host's cores share them
+#pragma omp parallel for schedule(static)
         for (int r = 0; r < n; r++) {
             if (r == c) continue;
             const double f = A[(long)r * n + c];
             if (f == 0.0) continue;
-            for (int l = 0; l < n; l++) {
-                A[(long)r * n + l] -= f * A[(long)c * n + l];
-                inv[(long)r * n + l] -= f * inv[(long)c * n + l];
-            }
+            for (int l = c; l < n; l++) A[(long)r * n + l] -= f * A[(long)c * n + l];
+            for (int l = 0; l < n; l++) inv[(long)r * n + l] -= f * inv[(long)c * n + l];
         }
     }
     return 1;

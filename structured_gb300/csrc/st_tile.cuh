@@ -25,8 +25,11 @@
 namespace st {
 
 constexpr int SW_THREADS = 256;
-// tile extents (cells): i-sweep TI_I x TJ_I, j-sweep TI_J x TJ_J
-constexpr int TI_I = 32, TJ_I = 8, TI_J = 8, TJ_J = 32;
+// tile extents (cells): i-sweep TI_I x TJ_I, j-sweep TI_J x TJ_J.  With 62 x 4
+// every phase has at most 256 items (slopes 64 x 4, faces 63 x 4, cells 62 x 4),
+// one per thread: no phase ends in a partly filled round while the FP64 pipe
+// waits at the barrier, and the halo recompute is 3 % (slopes), 1.6 % (faces).
+constexpr int TI_I = 62, TJ_I = 4, TI_J = 4, TJ_J = 62;
 // staged boxes of primitive records: i-sweep rows i0-1 .. i0+TI_I+2 (padded),
 // columns j0 .. j0+TJ_I+1; j-sweep rows i0 .. i0+TI_J+1, columns j0-1 .. j0+TJ_J+2
 constexpr int BI_I = TI_I + 4, BJ_I = TJ_I + 2, BI_J = TI_J + 2, BJ_J = TJ_J + 4;
