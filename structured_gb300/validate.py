@@ -169,9 +169,44 @@ def inversions(ni: int, nj: int, iters: int, out_dir: str | None, only: str | No
     return summaries
 
 
+def closure(data_dirs, steps: int, out_path: str | None, log=print):
+    """The learned-correction study over the inversion files of data_dirs:
+    the inversions' summaries, then training on all other cases that matched
+    their targets, on those at the held-out case's Reynolds number only, and on
+    the held-out case itself (the feature set's upper bound), each followed by
+    the held-out comparison of plain SA, the inverted-beta solve and the
+    learned solve."""
+    import glob
+    import shutil
+    import tempfile
+    from . import mlp
+    work = tempfile.mkdtemp()
+    summaries = []
+    for d in data_dirs:
+        for p in glob.glob(os.path.join(d, "inversion_*.npz")):
+            shutil.copy(p, work)
+        for p in glob.glob(os.path.join(d, "inversions_*.json")):
+            summaries += json.load(open(p))
+    out = {"inversions": summaries, "training": {}}
+    for mode in ("all", "same_re", "self"):
+        res, params, loss = mlp.run(work, steps=steps, train_mode=mode, log=log)
+        out["training"][mode] = res
+        if out_path:
+            with open(out_path, "w") as f:
+                json.dump(out, f, indent=1)
+            np.save(os.path.splitext(out_path)[0] + "_%s_params.npy" % mode, params)
+    if out_path:
+        # the held-out case's wall Cf: of its inverted-beta solution and its target
+        held = glob.glob(os.path.join(work, "inversion_%s_*.npz" % mlp.HELD_OUT))[0]
+        d = np.load(held)
+        np.savez(os.path.splitext(out_path)[0] + "_heldout.npz", cf_inv=d["cf_inv"], cf_target=d["cf_target"],
+                 name=os.path.basename(held))
+    return out
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("what", choices=["gradient", "inversion", "mlp"])
+    ap.add_argument("what", choices=["gradient", "inversion", "mlp", "closure"])
     ap.add_argument("--data", default=None)
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--iters", type=int, default=15)
@@ -185,6 +220,9 @@ def main(argv=None):
     a = ap.parse_args(argv)
     if a.what == "inversion":
         inversions(a.ni, a.nj, a.iters, a.out, a.only, log=lambda m: print(m, flush=True))
+        return 0
+    if a.what == "closure":
+        closure(a.data.split(","), a.steps, a.out, log=lambda m: print(m, flush=True))
         return 0
     if a.what == "mlp":
         from . import mlp
