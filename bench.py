@@ -257,6 +257,60 @@ def workload_config(args, grid):
             "l2": "inputs larger than L2 (q 336 MB, primitives 537 MB); no flush", "parallelism": "replicas"}
 
 
+CLOSURE = os.path.join(ROOT, "results", "closure_273x193")
+
+
+def closure_leg():
+    """The metric's second clause, on the learned-correction workload's
+    held-out case (Re_L 3e6, top inclined at -2 deg; 273x193, the grid of the
+    committed inversion study): a solve from freestream with the committed
+    network (trained on the other cases' inversions) fused into the SA source,
+    timed here, with its plate Cf error against the held-out case's
+    inverted-beta solution; beside it the field inversion's own wall time on
+    the same GPU type and plain SA's error, from the study's results file
+    (python -m structured_gb300.validate closure)."""
+    if not os.path.exists(CLOSURE + ".json"):
+        return None
+    import torch
+    from structured_gb300 import case as C
+    from structured_gb300 import inversion as inv
+    from structured_gb300 import mlp, workloads
+    from structured_gb300.solver import EulerEquation
+    study = json.load(open(CLOSURE + ".json"))
+    res = study["training"]["all"]
+    held = np.load(CLOSURE + "_heldout.npz")
+    params = np.load(CLOSURE + "_all_params.npy")
+    c = workloads.turbulent_plate(tempfile.gettempdir(), 273, 193, 3e6, -2.0, write_files=False)
+    g = C.flat_plate_grid(273, 193, h1=1e-7, ratio=1.05, top_angle_deg=-2.0)
+    eq = EulerEquation(c, g.xv, g.yv)
+    eq.mlp_init(0)
+    eq.mlp_set_params(params.astype(np.float32))
+    eq.mlp_set_normalization(np.array(res["feature_mean"], np.float32), np.array(res["feature_std"], np.float32))
+    eq.mlp_enable(True)
+    eq.set_state(C.freestream_state(c))
+    mask = inv.plate_mask(c, g.xv)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ok, hist = inv.converge(eq)
+    wall = time.perf_counter() - t0
+    cf, _ = eq.skin_friction()
+    eq.mlp_enable(False)
+    err = float(np.abs((cf - held["cf_inv"])[mask] / held["cf_inv"][mask]).max())
+    fi = res.get("field_inversion", {})
+    other = {m: {"train_cases": len(r["train_cases"]), "learned_cf_err_vs_inverted": r["learned"]["cf_err_vs_inverted"],
+                 "learned_solve_s": r["learned"]["wall_s"]}
+             for m, r in study["training"].items() if m != "all"}
+    return {"case": "turbulent plate 273x193, Re_L 3e6, top -2 deg (held out)",
+            "network": "trained on the eight other cases' inversions (results/closure_273x193_all_params.npy)",
+            "learned_solve_s": wall, "learned_steps": int(hist.shape[0] - 1) if hist is not None else None,
+            "learned_converged": bool(ok), "learned_cf_err_vs_inverted": err,
+            "plain_sa_cf_err_vs_inverted": res["plain_sa"]["cf_err_vs_inverted"],
+            "field_inversion_s": fi.get("wall_s"), "field_inversion_s_to_cf_err_1pct": fi.get("wall_s_to_cf_err_1pct"),
+            "other_training_sets": other,
+            "source": "learned solve timed here; inversion, plain-SA and other training sets from "
+                      "results/closure_273x193.json (python -m structured_gb300.validate closure)"}
+
+
 def run_ours(args, world, rank, local):
     import torch
     from structured_gb300 import build
@@ -405,6 +459,9 @@ def run_ours(args, world, rank, local):
         line["breakdown"]["residual_tiled_ms"] = t_ms
     if world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_sample(tb, 12.0, os.cpu_count() or 1, with_adj)
+    if world == 1 and tb == "sa" and not args.no_closure:
+        eq.close()
+        line["closure"] = closure_leg()
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -419,6 +476,7 @@ def main():
     ap.add_argument("--grid", choices=sorted(GRIDS), default="4097x2049")
     ap.add_argument("--turbulence", choices=["sa", "none"], default="sa")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-closure", action="store_true", help="skip the learned-correction solve")
     ap.add_argument("--residual-only", action="store_true", help="time the residual without the adjoint")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -61,6 +61,15 @@ def test_norms_and_skin_friction(gpu_lib, port_built, tmp_path):
     cf_ref, J_ref = PortCase(c, xv, yv).skin_friction(q)
     np.testing.assert_allclose(cf, cf_ref, rtol=1e-10, atol=1e-12 * np.abs(cf_ref).max())
     assert abs(J - J_ref) <= 1e-11 * abs(J_ref)
+    # the asynchronous form writes the same Cf and J (device reduction) to device buffers
+    import ctypes
+    import torch
+    cf_d = torch.zeros(c.nic, dtype=torch.float64, device="cuda")
+    J_d = torch.zeros(1, dtype=torch.float64, device="cuda")
+    assert eq.lib.st_skin_friction_device(eq.h, ctypes.c_void_p(cf_d.data_ptr()), ctypes.c_void_p(J_d.data_ptr())) == 0
+    _, _, stream = eq.device_state()
+    torch.cuda.ExternalStream(stream).synchronize()
+    assert np.array_equal(cf_d.cpu().numpy(), cf) and float(J_d.item()) == J
 
 
 def test_uniform_flow_preserved_on_device(gpu_lib, tmp_path):
