@@ -64,7 +64,7 @@ typedef struct st_case {
     int32_t turbulence;             /* ST_TURB_* */
     int32_t nbc;
     int32_t plate_vertex;           /* first no-slip wall vertex (objective) */
-    int32_t flux;                   /* ST_FLUX_*; the hand-written adjoint reverses Roe only */
+    int32_t flux;                   /* ST_FLUX_*; the hand-written adjoint reverses both */
     double rho_inf, u_inf, v_inf, p_inf, T_inf, mu_inf, pr_inf;
     double dpdx, dpdy;              /* [source] body force */
     double nu_tilde_inf;            /* SA freestream nu_tilde */

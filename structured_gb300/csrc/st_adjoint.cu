@@ -38,7 +38,7 @@ int ensure(st_ctx* x) {
 
 // Residual (when rhs != null) and adjoint in one sweep: the forward passes are
 // shared, and each face pass computes its flux and runs its reverse at once.
-template <int NQ, int ORDER>
+template <int NQ, int ORDER, int FLUX>
 int launch_fused(st_ctx* x, const double* psi, double* rhs, double* outq, double* outb) {
     cudaStream_t s = x->stream;
     const DevCase& dc = x->dc;
@@ -67,10 +67,10 @@ int launch_fused(st_ctx* x, const double* psi, double* rhs, double* outq, double
         k_cell_src<<<gc, 256, 0, s>>>(dc, x->P, x->Gi, x->Gj, x->beta, psi, x->srec, outb);
         stx::mark(x, "k_cell_src");
     }
-    k_face_fused<NQ, 0, ORDER><<<grid_for(x->nfi), 256, 0, s>>>(dc, x->P, x->lim, psi, x->srec, rhs ? x->Fi : nullptr,
+    k_face_fused<NQ, 0, ORDER, FLUX><<<grid_for(x->nfi), 256, 0, s>>>(dc, x->P, x->lim, psi, x->srec, rhs ? x->Fi : nullptr,
                                                                 x->arec_i);
     stx::mark(x, "k_face_fused_i");
-    k_face_fused<NQ, 1, ORDER><<<grid_for(x->nfj), 256, 0, s>>>(dc, x->P, x->lim, psi, x->srec, rhs ? x->Fj : nullptr,
+    k_face_fused<NQ, 1, ORDER, FLUX><<<grid_for(x->nfj), 256, 0, s>>>(dc, x->P, x->lim, psi, x->srec, rhs ? x->Fj : nullptr,
                                                                 x->arec_j);
     stx::mark(x, "k_face_fused_j");
     if (rhs) {
@@ -113,16 +113,20 @@ int fused_launches(const st_ctx* x, int order, bool with_rhs) {
     return n;
 }
 
+template <int FLUX>
+int run_fused_flux(st_ctx* x, const double* psi, double* rhs, double* outq, double* outb, int order) {
+    if (x->nq == 5)
+        return order == 2 ? launch_fused<5, 2, FLUX>(x, psi, rhs, outq, outb) : launch_fused<5, 1, FLUX>(x, psi, rhs, outq, outb);
+    return order == 2 ? launch_fused<4, 2, FLUX>(x, psi, rhs, outq, outb) : launch_fused<4, 1, FLUX>(x, psi, rhs, outq, outb);
+}
+
 int run_fused(st_ctx* x, const double* psi, double* rhs, double* outq, double* outb, int lhs) {
-    if (x->c.flux != ST_FLUX_ROE)
-        return stx::fail(ST_ERR_UNSUPPORTED, "adjoint: the hand-written reverse covers the Roe flux only");
     int rc = ensure(x);
     if (rc) return rc;
     const int order = lhs ? x->c.lhs_order : x->c.order;
     if (x->nq == 4 || !x->dc.viscous) ST_CUDA(cudaMemsetAsync(outb, 0, x->ncell * 8, x->stream));
-    if (x->nq == 5) rc = order == 2 ? launch_fused<5, 2>(x, psi, rhs, outq, outb) : launch_fused<5, 1>(x, psi, rhs, outq, outb);
-    else rc = order == 2 ? launch_fused<4, 2>(x, psi, rhs, outq, outb) : launch_fused<4, 1>(x, psi, rhs, outq, outb);
-    return rc;
+    return x->c.flux == ST_FLUX_AUSM ? run_fused_flux<ST_FLUX_AUSM>(x, psi, rhs, outq, outb, order)
+                                     : run_fused_flux<ST_FLUX_ROE>(x, psi, rhs, outq, outb, order);
 }
 
 }  // namespace

@@ -183,6 +183,96 @@ __device__ inline void roe_rev(const RoeTape& t, const double* fb, double* bl, d
     br[0] += rrht_; br[1] += urht_; br[2] += vrht_; br[3] += prht_;
 }
 
+// AUSM flux forward with the intermediates the reverse sweep needs (same
+// arithmetic as ausm_flux, src/model/flux.cpp:148-224): nx, ny the face normal
+// scaled by its length ds.
+struct AusmTape {
+    double rl, ul, vl, pl, rr, ur, vr, pr, nx, ny, ds;
+    double ids, al, ar, ial, iar, ml, mr, mhalf, phalf, ri, uv, h, m;
+    bool left;
+    double f[4];
+};
+
+__device__ inline double ausm_mach_d(double M, double s) {  // d ausm_mach / dM
+    return ::fabs(M) <= 1.0 ? 0.5 * s * (M + s) : 0.5 * (1.0 + s * sgn(M));
+}
+
+__device__ inline void ausm_fwd(AusmTape& t) {
+    t.ids = 1.0 / t.ds;
+    t.al = ::sqrt(GAMMA * t.pl * (1.0 / t.rl));
+    t.ar = ::sqrt(GAMMA * t.pr * (1.0 / t.rr));
+    t.ial = 1.0 / t.al;
+    t.iar = 1.0 / t.ar;
+    t.ml = (t.ul * t.nx + t.vl * t.ny) * t.ids * t.ial;
+    t.mr = (t.ur * t.nx + t.vr * t.ny) * t.ids * t.iar;
+    t.mhalf = ausm_mach(t.ml, 1.0) + ausm_mach(t.mr, -1.0);
+    t.phalf = ausm_pres(t.ml, t.pl, 1.0) + ausm_pres(t.mr, t.pr, -1.0);
+    t.left = t.mhalf >= 0.0;
+    const double r = t.left ? t.rl : t.rr, a = t.left ? t.al : t.ar, u = t.left ? t.ul : t.ur;
+    const double v = t.left ? t.vl : t.vr, p = t.left ? t.pl : t.pr;
+    t.ri = 1.0 / r;
+    t.uv = 0.5 * (u * u + v * v);
+    t.h = (p * OGM1 + r * t.uv + p) * t.ri;
+    t.m = r * a * t.mhalf * t.ds;
+    t.f[0] = t.m;
+    t.f[1] = t.m * u + t.phalf * t.nx;
+    t.f[2] = t.m * v + t.phalf * t.ny;
+    t.f[3] = t.m * t.h;
+}
+
+// d ausm_pres / dp and / dM on one side (s = +1 left, -1 right); above |M| = 1
+// the pressure split is p (1 + s sgn M) / 2, independent of M
+__device__ inline void ausm_pres_d(double M, double p, double s, double* dp, double* dM) {
+    if (::fabs(M) <= 1.0) {
+        const double a = M + s, b = 2.0 - s * M;
+        *dp = 0.25 * a * a * b;
+        *dM = 0.25 * p * (2.0 * a * b - s * a * a);
+    } else {
+        *dp = 0.5 * (M + s * ::fabs(M)) / M;
+        *dM = 0.0;
+    }
+}
+
+// Reverse sweep of ausm_fwd: fb[0..3] = adjoint of f; accumulates the adjoints
+// of the eight face states into bl[0..3], br[0..3].
+__device__ inline void ausm_rev(const AusmTape& t, const double* fb, double* bl, double* br) {
+    const double u = t.left ? t.ul : t.ur, v = t.left ? t.vl : t.vr, p = t.left ? t.pl : t.pr;
+    const double r = t.left ? t.rl : t.rr, a = t.left ? t.al : t.ar;
+    double m_ = fb[0] + fb[1] * u + fb[2] * v + fb[3] * t.h;
+    double u_ = fb[1] * t.m, v_ = fb[2] * t.m;
+    const double h_ = fb[3] * t.m;
+    const double phalf_ = fb[1] * t.nx + fb[2] * t.ny;
+    // h = (p / (gamma - 1) + r uv + p) / r
+    const double nh_ = h_ * t.ri;
+    double r_ = nh_ * t.uv - h_ * t.h * t.ri;
+    double p_ = nh_ * (OGM1 + 1.0);
+    const double uv_ = nh_ * r;
+    u_ += uv_ * u;
+    v_ += uv_ * v;
+    // m = r a mhalf ds
+    r_ += m_ * a * t.mhalf * t.ds;
+    double a_ = m_ * r * t.mhalf * t.ds;
+    const double mhalf_ = m_ * r * a * t.ds;
+    double ml_ = mhalf_ * ausm_mach_d(t.ml, 1.0), mr_ = mhalf_ * ausm_mach_d(t.mr, -1.0);
+    double dpl, dml, dpr, dmr;
+    ausm_pres_d(t.ml, t.pl, 1.0, &dpl, &dml);
+    ausm_pres_d(t.mr, t.pr, -1.0, &dpr, &dmr);
+    ml_ += phalf_ * dml;
+    mr_ += phalf_ * dmr;
+    double al_ = 0.0, ar_ = 0.0;
+    if (t.left) { bl[0] += r_; bl[1] += u_; bl[2] += v_; bl[3] += p_; al_ += a_; }
+    else { br[0] += r_; br[1] += u_; br[2] += v_; br[3] += p_; ar_ += a_; }
+    bl[3] += phalf_ * dpl;
+    br[3] += phalf_ * dpr;
+    // ml = (ul nx + vl ny) / (ds al)
+    const double cl = ml_ * t.ids * t.ial, cr = mr_ * t.ids * t.iar;
+    bl[1] += cl * t.nx; bl[2] += cl * t.ny; al_ -= ml_ * t.ml * t.ial;
+    br[1] += cr * t.nx; br[2] += cr * t.ny; ar_ -= mr_ * t.mr * t.iar;
+    // a = sqrt(gamma p / r): da/dp = a / (2p), da/dr = -a / (2r)
+    bl[3] += al_ * t.al * 0.5 / t.pl; bl[0] -= al_ * t.al * 0.5 / t.rl;
+    br[3] += ar_ * t.ar * 0.5 / t.pr; br[0] -= ar_ * t.ar * 0.5 / t.rr;
+}
+
 // Reverse of sa_source (same forward formulas); outputs adjoints of rho, nut,
 // mu, omega, |grad nut|^2 and beta for source adjoint sb.  Each quotient's
 // reciprocal is formed once (Newton-Raphson, st_common.cuh) and shared by the
@@ -347,8 +437,10 @@ static __global__ void __launch_bounds__(256) k_cell_src(DevCase c, const double
 // R2: one pass per face family that computes the face flux (for the
 // residual, when F != nullptr) and runs its reverse sweep in place, seeded by
 // the flux adjoint w(R) - w(L), w = psi / V (0 on ghost sides), and, with SA,
-// by the gradient-part adjoints of the two adjacent cells' sources.
-template <int NQ, int DIR, int ORDER>
+// by the gradient-part adjoints of the two adjacent cells' sources.  FLUX:
+// ST_FLUX_ROE or ST_FLUX_AUSM (a separate instantiation each, so the Roe pass
+// carries none of the AUSM code).
+template <int NQ, int DIR, int ORDER, int FLUX = ST_FLUX_ROE>
 __global__ void __launch_bounds__(256, 2) k_face_fused(DevCase c, const double* __restrict__ P,
                                                     const double* __restrict__ lim, const double* __restrict__ psi,
                                                     const double* __restrict__ srec, double* __restrict__ F,
@@ -385,22 +477,39 @@ __global__ void __launch_bounds__(256, 2) k_face_fused(DevCase c, const double* 
                 if (fi.limR) qR[k] -= lim[lim_off(c, DIR, LIM_SR, fi.phR) + k];
             }
         }
-        RoeTape rt;
-        rt.rlft = qL[0]; rt.ulft = qL[1]; rt.vlft = qL[2]; rt.plft = qL[3];
-        rt.rrht = qR[0]; rt.urht = qR[1]; rt.vrht = qR[2]; rt.prht = qR[3];
-        rt.r1 = gm[G_R1]; rt.r2 = gm[G_R2]; rt.aj = gm[G_AJ];
-        roe_fwd(rt);
-        double f[5] = {rt.f[0], rt.f[1], rt.f[2], rt.f[3], 0.0};
-        double bl[5] = {0, 0, 0, 0, 0}, br[5] = {0, 0, 0, 0, 0};
+        double f[5], bl[5] = {0, 0, 0, 0, 0}, br[5] = {0, 0, 0, 0, 0};
         double fcb[4] = {fb[0], fb[1], fb[2], fb[3]};
-        if (NQ == 5) {
-            const bool up = rt.f[0] >= 0.0;
-            const double nup = up ? qL[4] : qR[4];
-            f[4] = rt.f[0] * nup;
-            fcb[0] += fb[4] * nup;
-            if (up) bl[4] += fb[4] * rt.f[0]; else br[4] += fb[4] * rt.f[0];
+        // SA convection: the mass flux upwinds nu_tilde
+        auto sa_upwind = [&]() {
+            if (NQ == 5) {
+                const bool up = f[0] >= 0.0;
+                const double nup = up ? qL[4] : qR[4];
+                f[4] = f[0] * nup;
+                fcb[0] += fb[4] * nup;
+                if (up) bl[4] += fb[4] * f[0]; else br[4] += fb[4] * f[0];
+            } else {
+                f[4] = 0.0;
+            }
+        };
+        if constexpr (FLUX == ST_FLUX_AUSM) {
+            AusmTape at;
+            at.rl = qL[0]; at.ul = qL[1]; at.vl = qL[2]; at.pl = qL[3];
+            at.rr = qR[0]; at.ur = qR[1]; at.vr = qR[2]; at.pr = qR[3];
+            at.nx = gm[G_NX]; at.ny = gm[G_NY]; at.ds = 2.0 * gm[G_AJ];
+            ausm_fwd(at);
+            for (int k = 0; k < 4; k++) f[k] = at.f[k];
+            sa_upwind();
+            ausm_rev(at, fcb, bl, br);
+        } else {
+            RoeTape rt;
+            rt.rlft = qL[0]; rt.ulft = qL[1]; rt.vlft = qL[2]; rt.plft = qL[3];
+            rt.rrht = qR[0]; rt.urht = qR[1]; rt.vrht = qR[2]; rt.prht = qR[3];
+            rt.r1 = gm[G_R1]; rt.r2 = gm[G_R2]; rt.aj = gm[G_AJ];
+            roe_fwd(rt);
+            for (int k = 0; k < 4; k++) f[k] = rt.f[k];
+            sa_upwind();
+            roe_rev(rt, fcb, bl, br);
         }
-        roe_rev(rt, fcb, bl, br);
         if (c.viscous) {
             const double* pPa = P + fi.Pa; const double* pPb = P + fi.Pb;
             const double* pMa = P + fi.Ma; const double* pMb = P + fi.Mb;
@@ -555,6 +664,7 @@ __global__ void __launch_bounds__(256) k_gather(DevCase c, const double* __restr
         const double* self = P + idx * NP;
         double sd_r = 0.0, sd_n = 0.0, sd_m = 0.0;  // d (rho nut f_n) / d (rho, nut, mu) of this record
         if (NQ == 5 && c.viscous) sa_diff_d(self[P_RHO], self[P_NUT], self[P_MU], &sd_r, &sd_n, &sd_m);
+        double rnb_acc = 0.0;  // sum over the viscous stencils of the face-average adjoint of rho nut f_n
         auto visc = [&](const double* r, const double* gm, int role) {
             double wx, wy, co;
             if (role == 0) { wx = gm[G_WLX]; wy = gm[G_WLY]; co = 0.375; }
@@ -567,9 +677,8 @@ __global__ void __launch_bounds__(256) k_gather(DevCase c, const double* __restr
             acc[P_MU] += r[A_MUB] * co;
             if (NQ == 5) {
                 acc[P_MUT] += r[A_MUTB] * co;
-                acc[P_NUT] += r[A_DNDX] * wx + r[A_DNDY] * wy + r[A_RNB] * co * sd_n;
-                acc[P_RHO] += r[A_RNB] * co * sd_r;
-                acc[P_MU] += r[A_RNB] * co * sd_m;
+                acc[P_NUT] += r[A_DNDX] * wx + r[A_DNDY] * wy;
+                rnb_acc += r[A_RNB] * co;  // times this record's d(rho nut f_n) at the end
             }
         };
         // ---- i-faces (f, j): L=(f, j+1) R=(f+1, j+1) P=(f|f+1, j+2) M=(f|f+1, j)
@@ -641,6 +750,11 @@ __global__ void __launch_bounds__(256) k_gather(DevCase c, const double* __restr
                     if (r) visc(r, c.geo_j + ((size_t)is[t] * c.nj + gs[t]) * NGEO, roles[t]);
                 }
             }
+        }
+        if (NQ == 5 && c.viscous) {
+            acc[P_NUT] += rnb_acc * sd_n;
+            acc[P_RHO] += rnb_acc * sd_r;
+            acc[P_MU] += rnb_acc * sd_m;
         }
         const bool phys = ip >= 1 && ip <= c.nic && jp >= 1 && jp <= c.njc;
         if (NQ == 5 && phys && c.viscous) {

@@ -31,17 +31,11 @@ def eq_for(case, xv, yv):
 @pytest.mark.parametrize("lhs", [False, True])
 def test_vjp_matches_oracle_on_fixtures(gpu_lib, port_built, name, lhs):
     from oracle.port import PortCase
-    from structured_gb300.solver import StructuredError
     c, g = load_golden(name)
     eq = eq_for(c, g["xv"], g["yv"])
     port = PortCase(c, g["xv"], g["yv"])
     eq.set_state(g["q"])
     psi = np.random.default_rng(31).standard_normal(g["q"].shape)
-    if c.flux == "ausm":  # the hand-written reverse covers the Roe flux only
-        with pytest.raises(StructuredError) as e:
-            eq.vjp(psi, lhs=lhs)
-        assert e.value.code == -6  # ST_ERR_UNSUPPORTED
-        return
     oq, ob = eq.vjp(psi, lhs=lhs)
     rq, rb = port.vjp(g["q"], psi, lhs=lhs)
     assert close(oq, rq) < TOL
@@ -145,3 +139,36 @@ def test_sa_neg_vjp_matches_oracle(gpu_lib, port_built, tmp_path):
     rq, rb = PortCase(c, xv, yv).vjp(q, psi, beta)
     assert close(oq, rq) < TOL
     assert close(ob, rb) < TOL
+
+
+@pytest.mark.parametrize("mach", [0.3, 1.6])
+def test_ausm_sa_vjp_matches_oracle_and_jvp(gpu_lib, port_built, tmp_path, mach):
+    """The hand-written reverse of the AUSM flux (the reference's default,
+    src/model/flux.cpp:148-224) with SA, subsonic and supersonic (both branches
+    of the split Mach numbers and pressures): against the oracle's exact
+    transposed products, and by the dot-product identity with the device JVP."""
+    import torch
+    from oracle.port import PortCase
+    c = flat_plate(tmp_path, "ausm", 45, 29, turbulence="sa", reynolds=5e6, h1=1e-6, ratio=1.15, mach=mach)
+    c.flux = "ausm"
+    xv, yv = C.load_grid(c)
+    q = C.perturbed_state(c, 48)
+    rng = np.random.default_rng(49)
+    beta = 1.0 + 0.2 * rng.standard_normal((c.nic, c.njc))
+    psi = rng.standard_normal(q.shape)
+    eq = eq_for(c, xv, yv)
+    eq.set_state(q)
+    eq.set_beta(beta)
+    oq, ob = eq.vjp(psi)
+    rq, rb = PortCase(c, xv, yv).vjp(q, psi, beta)
+    assert close(oq, rq) < TOL
+    assert close(ob, rb) < TOL
+    v = torch.tensor(rng.standard_normal(q.shape) * np.abs(q).mean(axis=(0, 1)), device="cuda")
+    vb = torch.tensor(rng.standard_normal((c.nic, c.njc)), device="cuda")
+    jv = torch.empty_like(v)
+    eq.jvp_device(v.data_ptr(), jv.data_ptr(), vb.data_ptr())
+    torch.cuda.synchronize()
+    lhs = float((torch.tensor(psi, device="cuda") * jv).sum())
+    rhs = float((torch.tensor(oq, device="cuda") * v).sum() + (torch.tensor(ob, device="cuda") * vb).sum())
+    mag = float((torch.tensor(psi, device="cuda") * jv).abs().sum())
+    assert abs(lhs - rhs) <= 1e-11 * mag
