@@ -116,7 +116,8 @@ int st_create(const st_case* c, const double* xv, const double* yv, int device, 
 int st_destroy(st_ctx* ctx);
 int st_dims(const st_ctx* ctx, int* nic, int* njc, int* nq);
 
-/* State transfer (Solution::q).  Host buffers [nic][njc][nq]. */
+/* State transfer (Solution::q).  Host buffers [nic][njc][nq].  Synchronous;
+ * the copies run on the context's copy stream after the work already queued. */
 int st_set_state(st_ctx* ctx, const double* q_host);
 int st_get_state(st_ctx* ctx, double* q_host);
 /* SA production multiplier beta [nic][njc] (default 1). */
@@ -126,7 +127,10 @@ int st_get_wall_distance(st_ctx* ctx, double* d_host);
 /* Residual: EulerEquation::calc_residual(q, rhs, lhs)
  * (src/model/eulerequation.h:53, eulerequation.cpp:202-232), evaluated on the
  * context's state; lhs != 0 selects lhs_order.  rhs_host [nic][njc][nq] may be
- * NULL to keep the result on the device. */
+ * NULL to keep the result on the device.  The copy to rhs_host overlaps the
+ * last pass: the cell pass runs in up to 8 bands and each band goes out on
+ * the copy stream while the next computes (page-locked rhs_host lets the
+ * copies run asynchronously). */
 int st_residual(st_ctx* ctx, int lhs, double* rhs_host);
 /* Same on caller-provided device buffers (q_dev, rhs_dev: [nic][njc][nq]);
  * beta_dev may be NULL (beta = 1). */
@@ -177,7 +181,10 @@ int st_jvp_device(st_ctx* ctx, const double* v_dev, const double* vb_dev, double
  * on the context state (no tape, face fluxes recomputed).  Either output may
  * be NULL.  All device pointers. */
 int st_vjp_device(st_ctx* ctx, const double* psi_dev, double* out_q_dev, double* out_beta_dev, int lhs);
-/* Host-buffer variant (copies in the timed path). */
+/* Host-buffer variant.  psi goes in on the copy stream while the forward
+ * passes run; out_beta goes out as soon as it is final; out_q follows the
+ * last pass band by band.  Page-locked host buffers let the copies overlap
+ * the passes. */
 int st_vjp(st_ctx* ctx, const double* psi_host, double* out_q_host, double* out_beta_host, int lhs);
 /* Residual and adjoint of the same state in one sweep (the forward passes
  * are shared and each face pass computes its flux and its reverse at once):
@@ -185,7 +192,8 @@ int st_vjp(st_ctx* ctx, const double* psi_host, double* out_q_host, double* out_
  * rhs.  Device pointers; outputs may be NULL except rhs. */
 int st_residual_vjp_device(st_ctx* ctx, const double* psi_dev, double* rhs_dev, double* out_q_dev,
                            double* out_beta_dev, int lhs);
-/* Host-buffer variant of st_residual_vjp_device (on the context state). */
+/* Host-buffer variant of st_residual_vjp_device (on the context state), with
+ * the copies overlapped as in st_vjp; rhs goes out while the gather runs. */
 int st_residual_vjp(st_ctx* ctx, const double* psi_host, double* rhs_host, double* out_q_host,
                     double* out_beta_host, int lhs);
 /* Kernel launches one st_residual_vjp_device call makes. */

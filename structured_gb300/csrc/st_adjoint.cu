@@ -64,8 +64,16 @@ int launch_fused(st_ctx* x, const double* psi, double* rhs, double* outq, double
         k_face_grad<0><<<grid_for(x->nfi), 256, 0, s>>>(dc, x->P, x->Gi);
         k_face_grad<1><<<grid_for(x->nfj), 256, 0, s>>>(dc, x->P, x->Gj);
         stx::mark(x, "k_face_grad(i+j)");
+    }
+    // psi is first read below: a host-buffer call copies it in meanwhile
+    if (x->hio.psi_ready) ST_CUDA(cudaStreamWaitEvent(s, x->hio.psi_ready, 0));
+    if (NQ == 5 && dc.viscous) {
         k_cell_src<<<gc, 256, 0, s>>>(dc, x->P, x->Gi, x->Gj, x->beta, psi, x->srec, outb);
         stx::mark(x, "k_cell_src");
+    }
+    if (x->hio.outb) {  // outb is final (set above or zeroed before the pipeline)
+        const int rc = stx::copy_out(x, x->xev[2], x->hio.outb, outb, x->ncell * 8);
+        if (rc) return rc;
     }
     k_face_fused<NQ, 0, ORDER, FLUX><<<grid_for(x->nfi), 256, 0, s>>>(dc, x->P, x->lim, psi, x->srec, rhs ? x->Fi : nullptr,
                                                                 x->arec_i);
@@ -76,6 +84,10 @@ int launch_fused(st_ctx* x, const double* psi, double* rhs, double* outq, double
     if (rhs) {
         k_cell_res<NQ><<<gc, 256, 0, s>>>(dc, x->Fi, x->Fj, x->srec, rhs);
         stx::mark(x, "k_cell_res");
+        if (x->hio.rhs) {  // copied out while the gather runs
+            const int rc = stx::copy_out(x, x->xev[3], x->hio.rhs, rhs, x->ncell * NQ * 8);
+            if (rc) return rc;
+        }
     }
     k_gather<NQ, ORDER><<<grid_for(x->npad), 256, 0, s>>>(dc, x->P, x->arec_i, x->arec_j, x->srec, x->Pbar);
     stx::mark(x, "k_gather");
@@ -89,7 +101,12 @@ int launch_fused(st_ctx* x, const double* psi, double* rhs, double* outq, double
         }
     }
     stx::mark(x, "k_bc_adj");
-    k_prim_adj<NQ><<<gc, 256, 0, s>>>(dc, x->q, x->P, x->Pbar, outq);
+    {
+        const int rc = stx::run_banded(x, x->hio.outq, outq, NQ, [&](size_t f, size_t l) {
+            k_prim_adj<NQ><<<grid_for(l - f), 256, 0, s>>>(dc, x->q, x->P, x->Pbar, outq, f, l);
+        });
+        if (rc) return rc;
+    }
     stx::mark(x, "k_prim_adj");
     ST_LAUNCH_CHECK("residual/adjoint launch");
     return ST_OK;
@@ -135,6 +152,48 @@ namespace stx {
 int ensure_adjoint_buffers(st_ctx* x) { return ensure(x); }
 }  // namespace stx
 
+namespace {
+// Enqueues a host-buffer VJP with its copies overlapped (see host_vjp).
+int host_vjp_enqueue(st_ctx* x, const double* psi_host, double* rhs_host, double* outq_host, double* outb_host,
+                     int lhs, bool with_rhs) {
+    const size_t nqb = x->ncell * x->nq * 8;
+    // the copy stream starts after the work already queued (which may still read psi_tmp)
+    ST_CUDA(cudaEventRecord(x->xev[0], x->stream));
+    ST_CUDA(cudaStreamWaitEvent(x->xfer, x->xev[0], 0));
+    ST_CUDA(cudaMemcpyAsync(x->psi_tmp, psi_host, nqb, cudaMemcpyHostToDevice, x->xfer));
+    ST_CUDA(cudaEventRecord(x->xev[1], x->xfer));
+    x->hio.psi_ready = x->xev[1];
+    x->hio.rhs = with_rhs ? rhs_host : nullptr;
+    x->hio.outq = outq_host;
+    x->hio.outb = outb_host;
+    const int rc = with_rhs ? st_residual_vjp_device(x, x->psi_tmp, x->rhs, x->outq_tmp, x->outb_tmp, lhs)
+                            : st_vjp_device(x, x->psi_tmp, x->outq_tmp, x->outb_tmp, lhs);
+    x->hio = {};
+    if (rc) return rc;
+    if (with_rhs) x->have_residual = true;
+    return ST_OK;
+}
+
+// Host-buffer VJP (and residual): psi goes in on the copy stream while the
+// forward passes run, and the pipeline waits for it before its first read of
+// psi; the beta product and the residual go out on that stream as soon as
+// they are final, during the gather; k_prim_adj runs in bands whose outputs
+// go out while the next band computes.  Both streams are drained before the
+// call returns, on errors too, so the caller's buffers are free again.
+int host_vjp(st_ctx* x, const double* psi_host, double* rhs_host, double* outq_host, double* outb_host, int lhs,
+             bool with_rhs) {
+    int rc = ensure(x);
+    if (rc) return rc;
+    rc = host_vjp_enqueue(x, psi_host, rhs_host, outq_host, outb_host, lhs, with_rhs);
+    const cudaError_t e1 = cudaStreamSynchronize(x->xfer);
+    const cudaError_t e2 = cudaStreamSynchronize(x->stream);
+    if (rc) return rc;
+    if (e1 != cudaSuccess) return stx::cuda_fail(e1, "cudaStreamSynchronize (copy stream)");
+    if (e2 != cudaSuccess) return stx::cuda_fail(e2, "cudaStreamSynchronize");
+    return ST_OK;
+}
+}  // namespace
+
 extern "C" {
 
 int st_vjp_device(st_ctx* x, const double* psi, double* outq, double* outb, int lhs) {
@@ -163,30 +222,12 @@ int st_residual_vjp_device(st_ctx* x, const double* psi, double* rhs, double* ou
 
 int st_vjp(st_ctx* x, const double* psi_host, double* outq_host, double* outb_host, int lhs) {
     if (!x || !psi_host) return fail(ST_ERR_ARG, "st_vjp: null argument");
-    int rc = ensure(x);
-    if (rc) return rc;
-    ST_CUDA(cudaMemcpyAsync(x->psi_tmp, psi_host, x->ncell * x->nq * 8, cudaMemcpyHostToDevice, x->stream));
-    rc = st_vjp_device(x, x->psi_tmp, x->outq_tmp, x->outb_tmp, lhs);
-    if (rc) return rc;
-    if (outq_host) ST_CUDA(cudaMemcpyAsync(outq_host, x->outq_tmp, x->ncell * x->nq * 8, cudaMemcpyDeviceToHost, x->stream));
-    if (outb_host) ST_CUDA(cudaMemcpyAsync(outb_host, x->outb_tmp, x->ncell * 8, cudaMemcpyDeviceToHost, x->stream));
-    ST_CUDA(cudaStreamSynchronize(x->stream));
-    return ST_OK;
+    return host_vjp(x, psi_host, nullptr, outq_host, outb_host, lhs, false);
 }
 
 int st_residual_vjp(st_ctx* x, const double* psi_host, double* rhs_host, double* outq_host, double* outb_host, int lhs) {
     if (!x || !psi_host) return fail(ST_ERR_ARG, "st_residual_vjp: null argument");
-    int rc = ensure(x);
-    if (rc) return rc;
-    ST_CUDA(cudaMemcpyAsync(x->psi_tmp, psi_host, x->ncell * x->nq * 8, cudaMemcpyHostToDevice, x->stream));
-    rc = st_residual_vjp_device(x, x->psi_tmp, x->rhs, x->outq_tmp, x->outb_tmp, lhs);
-    if (rc) return rc;
-    x->have_residual = true;
-    if (rhs_host) ST_CUDA(cudaMemcpyAsync(rhs_host, x->rhs, x->ncell * x->nq * 8, cudaMemcpyDeviceToHost, x->stream));
-    if (outq_host) ST_CUDA(cudaMemcpyAsync(outq_host, x->outq_tmp, x->ncell * x->nq * 8, cudaMemcpyDeviceToHost, x->stream));
-    if (outb_host) ST_CUDA(cudaMemcpyAsync(outb_host, x->outb_tmp, x->ncell * 8, cudaMemcpyDeviceToHost, x->stream));
-    ST_CUDA(cudaStreamSynchronize(x->stream));
-    return ST_OK;
+    return host_vjp(x, psi_host, rhs_host, outq_host, outb_host, lhs, true);
 }
 
 int st_launch_counts(st_ctx* x, int lhs, int* residual, int* vjp) {

@@ -1009,9 +1009,10 @@ static __global__ void __launch_bounds__(256) k_tape_ring(DevCase c, const doubl
 // R6: primitives -> conserved adjoint per physical cell (reverse of k_prim).
 template <int NQ>
 __global__ void __launch_bounds__(256) k_prim_adj(DevCase c, const double* __restrict__ q, const double* __restrict__ P,
-                                                  const double* __restrict__ Pbar, double* __restrict__ out) {
-    const size_t n = (size_t)c.nic * c.njc;
-    for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += (size_t)gridDim.x * blockDim.x) {
+                                                  const double* __restrict__ Pbar, double* __restrict__ out,
+                                                  size_t first, size_t n) {
+    for (size_t idx = first + (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n;
+         idx += (size_t)gridDim.x * blockDim.x) {
         const int i = (int)(idx / c.njc), j = (int)(idx % c.njc);
         const double* Q = q + idx * NQ;
         const double* p = P + pidx(c, i + 1, j + 1);

@@ -9,6 +9,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "st_context.h"
@@ -374,11 +375,23 @@ int launch_forward(st_ctx* x, const DevCase& dc, const T* q, const T* beta, T* P
         k_face<T, NQ, 1, 1><<<grid_for(x->nfj), 256, 0, s>>>(dc, P, lim, Fj, Gj);
         stx::mark(x, "k_face_j");
     }
-    if constexpr (NQ == 5) {
-        if (dc.mlp_wb) k_cell<T, NQ, true><<<gc, 256, 0, s>>>(dc, P, Fi, Fj, Gi, Gj, beta, rhs);
-        else k_cell<T, NQ><<<gc, 256, 0, s>>>(dc, P, Fi, Fj, Gi, Gj, beta, rhs);
+    // the host-buffer residual copies the state's residual out band by band
+    double* dst = nullptr;
+    if constexpr (std::is_same_v<T, double>) dst = rhs == x->rhs ? x->hio.rhs : nullptr;
+    auto cell = [&](size_t f, size_t l) {
+        const unsigned g = grid_for(l - f);
+        if constexpr (NQ == 5) {
+            if (dc.mlp_wb) k_cell<T, NQ, true><<<g, 256, 0, s>>>(dc, P, Fi, Fj, Gi, Gj, beta, rhs, f, l);
+            else k_cell<T, NQ><<<g, 256, 0, s>>>(dc, P, Fi, Fj, Gi, Gj, beta, rhs, f, l);
+        } else {
+            k_cell<T, NQ><<<g, 256, 0, s>>>(dc, P, Fi, Fj, Gi, Gj, beta, rhs, f, l);
+        }
+    };
+    if constexpr (std::is_same_v<T, double>) {
+        const int rc = stx::run_banded(x, dst, rhs, NQ, cell);
+        if (rc) return rc;
     } else {
-        k_cell<T, NQ><<<gc, 256, 0, s>>>(dc, P, Fi, Fj, Gi, Gj, beta, rhs);
+        cell(0, x->ncell);
     }
     stx::mark(x, "k_cell");
     ST_LAUNCH_CHECK("residual launch");
@@ -408,6 +421,10 @@ int launch_tiled(st_ctx* x, const double* q, const double* beta, double* rhs, in
         k_sweep_j<NQ, 1><<<gj, SW_THREADS, SWEEP_SMEM_J, s>>>(dc, x->tmap_j, x->Gi, beta, rhs);
     }
     stx::mark(x, "k_sweep_j");
+    if (x->hio.rhs && rhs == x->rhs) {
+        const int rc = stx::copy_out(x, x->xev[3], x->hio.rhs, rhs, x->ncell * NQ * 8);
+        if (rc) return rc;
+    }
     ST_LAUNCH_CHECK("tiled residual launch");
     return ST_OK;
 }
@@ -606,6 +623,9 @@ int st_create(const st_case* c, const double* xv, const double* yv, int device, 
     if (rc != ST_OK) { st_destroy(x); return rc; }
     cudaStreamCreateWithFlags(&x->stream, cudaStreamNonBlocking);
     for (auto& e : x->ev) cudaEventCreate(&e);
+    cudaStreamCreateWithFlags(&x->xfer, cudaStreamNonBlocking);
+    for (auto& e : x->xev) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+    for (auto& e : x->band_ev) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
     std::vector<DevBC> dbc(std::max(1, c->nbc));
     for (int b = 0; b < c->nbc; b++)
         dbc[b] = DevBC{c->bcs[b].type, c->bcs[b].face, c->bcs[b].start, c->bcs[b].end, c->bcs[b].u, c->bcs[b].v, c->bcs[b].T};
@@ -721,7 +741,10 @@ int st_destroy(st_ctx* x) {
     float* fbufs[] = {x->mlp_wf, x->mlp_master, x->mlp_loss, x->mlp_part};
     for (float* b : fbufs) if (b) cudaFree(b);
     for (auto& e : x->ev) if (e) cudaEventDestroy(e);
+    for (auto& e : x->xev) if (e) cudaEventDestroy(e);
+    for (auto& e : x->band_ev) if (e) cudaEventDestroy(e);
     if (x->stream) cudaStreamDestroy(x->stream);
+    if (x->xfer) cudaStreamDestroy(x->xfer);
     delete x;
     return ST_OK;
 }
@@ -736,30 +759,22 @@ int st_dims(const st_ctx* x, int* nic, int* njc, int* nq) {
 
 int st_set_state(st_ctx* x, const double* q) {
     if (!x || !q) return fail(ST_ERR_ARG, "st_set_state: null argument");
-    ST_CUDA(cudaMemcpyAsync(x->q, q, x->ncell * x->nq * 8, cudaMemcpyHostToDevice, x->stream));
-    ST_CUDA(cudaStreamSynchronize(x->stream));
-    return ST_OK;
+    return stx::copy_sync(x, x->q, q, x->ncell * x->nq * 8, cudaMemcpyHostToDevice);
 }
 
 int st_get_state(st_ctx* x, double* q) {
     if (!x || !q) return fail(ST_ERR_ARG, "st_get_state: null argument");
-    ST_CUDA(cudaMemcpyAsync(q, x->q, x->ncell * x->nq * 8, cudaMemcpyDeviceToHost, x->stream));
-    ST_CUDA(cudaStreamSynchronize(x->stream));
-    return ST_OK;
+    return stx::copy_sync(x, q, x->q, x->ncell * x->nq * 8, cudaMemcpyDeviceToHost);
 }
 
 int st_set_beta(st_ctx* x, const double* b) {
     if (!x || !b) return fail(ST_ERR_ARG, "st_set_beta: null argument");
-    ST_CUDA(cudaMemcpyAsync(x->beta, b, x->ncell * 8, cudaMemcpyHostToDevice, x->stream));
-    ST_CUDA(cudaStreamSynchronize(x->stream));
-    return ST_OK;
+    return stx::copy_sync(x, x->beta, b, x->ncell * 8, cudaMemcpyHostToDevice);
 }
 
 int st_get_wall_distance(st_ctx* x, double* d) {
     if (!x || !d) return fail(ST_ERR_ARG, "st_get_wall_distance: null argument");
-    ST_CUDA(cudaMemcpyAsync(d, x->wd, x->ncell * 8, cudaMemcpyDeviceToHost, x->stream));
-    ST_CUDA(cudaStreamSynchronize(x->stream));
-    return ST_OK;
+    return stx::copy_sync(x, d, x->wd, x->ncell * 8, cudaMemcpyDeviceToHost);
 }
 
 int st_residual_device(st_ctx* x, const double* q_dev, const double* beta_dev, double* rhs_dev, int lhs) {
@@ -772,13 +787,19 @@ int st_residual_device(st_ctx* x, const double* q_dev, const double* beta_dev, d
     return ST_OK;
 }
 
+// The residual goes out on the copy stream: band by band behind the per-stage
+// cell pass, or whole after the tiled sweeps.
 int st_residual(st_ctx* x, int lhs, double* rhs_host) {
     if (!x) return fail(ST_ERR_ARG, "st_residual: null context");
-    int rc = st_residual_device(x, x->q, x->beta, x->rhs, lhs);
+    x->hio.rhs = rhs_host;
+    const int rc = st_residual_device(x, x->q, x->beta, x->rhs, lhs);
+    x->hio = {};
+    const cudaError_t e1 = cudaStreamSynchronize(x->xfer);
+    const cudaError_t e2 = cudaStreamSynchronize(x->stream);
     if (rc) return rc;
+    if (e1 != cudaSuccess) return stx::cuda_fail(e1, "cudaStreamSynchronize (copy stream)");
+    if (e2 != cudaSuccess) return stx::cuda_fail(e2, "cudaStreamSynchronize");
     x->have_residual = true;
-    if (rhs_host) ST_CUDA(cudaMemcpyAsync(rhs_host, x->rhs, x->ncell * x->nq * 8, cudaMemcpyDeviceToHost, x->stream));
-    ST_CUDA(cudaStreamSynchronize(x->stream));
     return ST_OK;
 }
 
@@ -787,7 +808,7 @@ int st_dt(st_ctx* x, double cfl, double* dt_host) {
     if (x->nq == 5) k_dt<5><<<grid_for(x->ncell), 256, 0, x->stream>>>(x->dc, x->q, x->dsmin_d, cfl, x->dt);
     else k_dt<4><<<grid_for(x->ncell), 256, 0, x->stream>>>(x->dc, x->q, x->dsmin_d, cfl, x->dt);
     ST_LAUNCH_CHECK("k_dt");
-    if (dt_host) ST_CUDA(cudaMemcpyAsync(dt_host, x->dt, x->ncell * x->nq * 8, cudaMemcpyDeviceToHost, x->stream));
+    if (dt_host) return stx::copy_sync(x, dt_host, x->dt, x->ncell * x->nq * 8, cudaMemcpyDeviceToHost);
     ST_CUDA(cudaStreamSynchronize(x->stream));
     return ST_OK;
 }

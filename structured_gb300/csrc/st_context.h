@@ -3,6 +3,7 @@
 #include <cuda.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <string>
 #include <vector>
 
@@ -83,6 +84,22 @@ struct st_ctx {
     bool tile_ok = false;
     int res_path = 0;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    // host-buffer entry points (st_residual, st_vjp, st_residual_vjp): the
+    // host<->device copies run on their own stream so that they overlap the
+    // pipeline (the host link moves about 0.2 TB/s each way).  hio is set
+    // only during such a call.  The pipeline waits on hio.psi_ready before
+    // its first read of psi; it queues the copy of each output to its host
+    // destination as soon as the output is final; and its last per-cell pass
+    // (k_cell, k_prim_adj) runs in bands, each band's output copied while
+    // the next band computes.
+    struct HostIO {
+        cudaEvent_t psi_ready = nullptr;
+        double *rhs = nullptr, *outq = nullptr, *outb = nullptr;
+    } hio;
+    cudaStream_t xfer = nullptr;
+    cudaEvent_t xev[4] = {nullptr, nullptr, nullptr, nullptr};
+    static constexpr int kBands = 8;
+    cudaEvent_t band_ev[kBands] = {};
     // per-launch profiling (st_profile_pipeline): an event after each launch
     bool prof_on = false;
     int prof_n = 0;
@@ -124,6 +141,43 @@ inline void mark(st_ctx* x, const char* name) {
 // the per-face passes, which also leave the face fluxes and gradient parts in
 // Fi/Fj/Gi/Gj for callers that read them.
 int run_residual(st_ctx* ctx, const double* q, const double* beta, double* rhs, int order);
+// Queues the copy of `bytes` from device src to host dst on the copy stream,
+// after the work queued so far on the context stream (ev: a free event).
+inline int copy_out(st_ctx* x, cudaEvent_t ev, double* dst, const double* src, size_t bytes) {
+    ST_CUDA(cudaEventRecord(ev, x->stream));
+    ST_CUDA(cudaStreamWaitEvent(x->xfer, ev, 0));
+    ST_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, x->xfer));
+    return ST_OK;
+}
+// Synchronous copy between host memory and the context's device buffers: on
+// the copy stream, after the work queued so far on the context stream.  Bulk
+// host copies stay off the context stream: after one there, the next
+// host-buffer call's copy of psi was measured not to overlap the forward
+// passes (1.6 ms more per call at 4097x2049).
+inline int copy_sync(st_ctx* x, void* dst, const void* src, size_t bytes, cudaMemcpyKind kind) {
+    ST_CUDA(cudaEventRecord(x->xev[0], x->stream));
+    ST_CUDA(cudaStreamWaitEvent(x->xfer, x->xev[0], 0));
+    ST_CUDA(cudaMemcpyAsync(dst, src, bytes, kind, x->xfer));
+    ST_CUDA(cudaStreamSynchronize(x->xfer));
+    return ST_OK;
+}
+// Runs a per-cell pass launch(first, last) over the cells [0, ncell); with a
+// host destination (dst non-null) in up to kBands bands, each band's nq
+// doubles per cell copied from dev to dst while the next band computes.
+template <class F>
+int run_banded(st_ctx* x, double* dst, const double* dev, int nq, F&& launch) {
+    const size_t n = x->ncell;
+    const int nb = dst ? (int)std::min<size_t>(st_ctx::kBands, (n + 65535) / 65536) : 1;
+    for (int b = 0; b < nb; b++) {
+        const size_t f = n * b / nb, l = n * (b + 1) / nb;
+        launch(f, l);
+        if (dst) {
+            int rc = copy_out(x, x->band_ev[b], dst + f * nq, dev + f * nq, (l - f) * nq * 8);
+            if (rc) return rc;
+        }
+    }
+    return ST_OK;
+}
 int run_residual_faces(st_ctx* ctx, const double* q, const double* beta, double* rhs, int order);
 // forward-mode JVP of the order-`order` residual at the context state (async);
 // freeze_nonlocal holds the periodic and wake ghosts' tangents at zero (the

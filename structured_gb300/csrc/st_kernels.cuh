@@ -560,15 +560,16 @@ __device__ inline T sa_source(T rho, T nut, T mu, double d, T omega, T gnut2, T 
 // MLP: beta of each cell from the learned correction (st_mlp.cuh), evaluated
 // in-kernel 32 cells per warp; the loop then runs over whole-warp tiles so
 // that every lane reaches the warp-wide MMAs.
+// The pass covers the cells [first, n) (a band of the grid when the host
+// call copies the residual out band by band).
 template <class T, int NQ, bool MLP = false>
 __global__ void __launch_bounds__(256) k_cell(DevCase c, const T* __restrict__ P, const T* __restrict__ Fi,
                                               const T* __restrict__ Fj, const T* __restrict__ Gi,
                                               const T* __restrict__ Gj, const T* __restrict__ beta,
-                                              T* __restrict__ rhs) {
-    const size_t n = (size_t)c.nic * c.njc;
+                                              T* __restrict__ rhs, size_t first, size_t n) {
     const size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (size_t base = (size_t)blockIdx.x * blockDim.x + (MLP ? (threadIdx.x & ~31u) : threadIdx.x); base < n;
-         base += stride) {
+    for (size_t base = first + (size_t)blockIdx.x * blockDim.x + (MLP ? (threadIdx.x & ~31u) : threadIdx.x);
+         base < n; base += stride) {
         const size_t idx = MLP ? base + (threadIdx.x & 31) : base;
         float mlp_beta = 1.f;
         if constexpr (MLP) {

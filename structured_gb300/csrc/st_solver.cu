@@ -1078,9 +1078,7 @@ int st_jacobian_assemble(st_ctx* x, int lhs) {
 int st_jacobian_blocks(st_ctx* x, double* blocks_host) {
     if (!x || !blocks_host) return fail(ST_ERR_ARG, "st_jacobian_blocks: null argument");
     if (!x->jac) return fail(ST_ERR_ARG, "st_jacobian_blocks: no Jacobian assembled");
-    ST_CUDA(cudaMemcpyAsync(blocks_host, x->jac, x->ncell * NOFF * x->nq * x->nq * 8, cudaMemcpyDeviceToHost, x->stream));
-    ST_CUDA(cudaStreamSynchronize(x->stream));
-    return ST_OK;
+    return stx::copy_sync(x, blocks_host, x->jac, x->ncell * NOFF * x->nq * x->nq * 8, cudaMemcpyDeviceToHost);
 }
 
 int st_jacobian_apply_device(st_ctx* x, const double* v_dev, double* out_dev, int transpose) {
@@ -1278,13 +1276,13 @@ int st_cf_gradient_device(st_ctx* x, const double* w_host, double* grad_dev) {
         k_bc_taped<5><<<1, 1024, 0, s>>>(dc, x->P, x->tape);
         k_cf_adj<<<(2 * (nic + 2) + 255) / 256, 256, 0, s>>>(dc, x->cf, x->c.mu_inf / qinf, x->Pbar);
         k_bc_adj<5><<<1, 1024, 0, s>>>(dc, x->P, x->tape, x->Pbar);
-        k_prim_adj<5><<<grid_for(x->ncell), 256, 0, s>>>(dc, x->q, x->P, x->Pbar, grad_dev);
+        k_prim_adj<5><<<grid_for(x->ncell), 256, 0, s>>>(dc, x->q, x->P, x->Pbar, grad_dev, 0, x->ncell);
     } else {
         k_prim<double, 4><<<grid_for(x->ncell), 256, 0, s>>>(dc, x->q, x->P);
         k_bc_taped<4><<<1, 1024, 0, s>>>(dc, x->P, x->tape);
         k_cf_adj<<<(2 * (nic + 2) + 255) / 256, 256, 0, s>>>(dc, x->cf, x->c.mu_inf / qinf, x->Pbar);
         k_bc_adj<4><<<1, 1024, 0, s>>>(dc, x->P, x->tape, x->Pbar);
-        k_prim_adj<4><<<grid_for(x->ncell), 256, 0, s>>>(dc, x->q, x->P, x->Pbar, grad_dev);
+        k_prim_adj<4><<<grid_for(x->ncell), 256, 0, s>>>(dc, x->q, x->P, x->Pbar, grad_dev, 0, x->ncell);
     }
     ST_LAUNCH_CHECK("cf gradient");
     ST_CUDA(cudaStreamSynchronize(s));
