@@ -5,6 +5,8 @@ Re_L=5e6, SA with beta = 1, J = drag on the plate):
   python -m structured_gb300.validate gradient [--cells 64] [--out file.json]
   python -m structured_gb300.validate inversion [--ni --nj --iters] [--out dir]
   python -m structured_gb300.validate mlp --data dir [--steps] [--out file.json]
+  python -m structured_gb300.validate closure --data dirs [--steps] [--out file.json]
+  python -m structured_gb300.validate heldout [--ni --nj --iters --study] [--out file.json]
 
 1. pseudo-time Newton from freestream to steady state;
 2. dJ/dbeta by one adjoint solve;
@@ -204,9 +206,72 @@ def closure(data_dirs, steps: int, out_path: str | None, log=print):
     return out
 
 
+def heldout(ni: int, nj: int, iters: int, study: str, out_path: str | None, log=print):
+    """The learned-correction workload's held-out case (Re_L 3e6, top inclined
+    at -2 deg) on an ni x nj grid.  Plain SA and the learned solve both start
+    from freestream and are timed.  The learned solve uses the network of the
+    study `study`, trained on the eight other cases' inversions at the
+    study's grid.  Then the case's own field inversion runs, and the plate Cf
+    of both solves is compared with the inverted-beta solution.  out_path (a
+    JSON) is written after each stage, and an .npz beside it holds the wall
+    Cf arrays."""
+    import torch
+    from . import case as C
+    from . import inversion as inv
+    from . import workloads
+    from .solver import EulerEquation
+    re_l, ang = 3e6, -2.0
+    res = json.load(open(study + ".json"))["training"]["all"]
+    params = np.load(study + "_all_params.npy")
+    out = {"case": "turbulent plate %dx%d, Re_L %.0e, top %+.0f deg (held out)" % (ni, nj, re_l, ang),
+           "network": os.path.basename(study) + "_all_params.npy", "network_train_cases": res["train_cases"]}
+
+    def save():
+        if out_path:
+            with open(out_path, "w") as f:
+                json.dump(out, f, indent=1)
+
+    c = workloads.turbulent_plate(tempfile.mkdtemp(), ni, nj, re_l, ang, write_files=False)
+    g = C.flat_plate_grid(ni, nj, h1=1e-7, ratio=1.05, top_angle_deg=ang)
+    mask = inv.plate_mask(c, g.xv)
+    eq = EulerEquation(c, g.xv, g.yv)
+    cfs = {}
+    for label, learned in (("plain_sa", False), ("learned", True)):
+        if learned:
+            eq.mlp_init(0)
+            eq.mlp_set_params(params.astype(np.float32))
+            eq.mlp_set_normalization(np.array(res["feature_mean"], np.float32), np.array(res["feature_std"], np.float32))
+            eq.mlp_enable(True)
+        eq.set_state(C.freestream_state(c))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ok, hist = inv.converge(eq)
+        wall = time.perf_counter() - t0
+        cfs[label] = eq.skin_friction()[0]
+        out[label] = {"solve_s": wall, "converged": bool(ok),
+                      "steps": int(hist.shape[0] - 1) if hist is not None else None}
+        log("%s: %s" % (label, json.dumps(out[label])))
+        save()
+    eq.mlp_enable(False)
+    eq.close()
+    summary, arrays = inv.run_case(re_l, ang, ni, nj, max_iter=iters, log=log)
+    cf_inv = arrays["cf_inv"]
+    err = lambda cf: float(np.abs((cf - cf_inv)[mask] / cf_inv[mask]).max())
+    out["inversion"] = summary
+    out["plain_sa"]["cf_err_vs_inverted"] = err(cfs["plain_sa"])
+    out["learned"]["cf_err_vs_inverted"] = err(cfs["learned"])
+    log("[heldout] " + json.dumps(out))
+    save()
+    if out_path:
+        np.savez_compressed(os.path.splitext(out_path)[0] + ".npz", cf_inv=cf_inv, cf_target=arrays["cf_target"],
+                            cf_plain=cfs["plain_sa"], cf_learned=cfs["learned"], iter_wall_s=arrays["iter_wall_s"],
+                            iter_cf=arrays["iter_cf"])
+    return out
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("what", choices=["gradient", "inversion", "mlp", "closure"])
+    ap.add_argument("what", choices=["gradient", "inversion", "mlp", "closure", "heldout"])
     ap.add_argument("--data", default=None)
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--iters", type=int, default=15)
@@ -217,7 +282,12 @@ def main(argv=None):
     ap.add_argument("--tangent", type=int, default=8)
     ap.add_argument("--out", default=None)
     ap.add_argument("--train", default="all", choices=["all", "same_re", "self"])
+    ap.add_argument("--study", default=os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                                                    "results", "closure_273x193"))
     a = ap.parse_args(argv)
+    if a.what == "heldout":
+        heldout(a.ni, a.nj, a.iters, a.study, a.out, log=lambda m: print(m, flush=True))
+        return 0
     if a.what == "inversion":
         inversions(a.ni, a.nj, a.iters, a.out, a.only, log=lambda m: print(m, flush=True))
         return 0
