@@ -212,9 +212,10 @@ def heldout(ni: int, nj: int, iters: int, study: str, out_path: str | None, log=
     from freestream and are timed.  The learned solve uses the network of the
     study `study`, trained on the eight other cases' inversions at the
     study's grid.  Then the case's own field inversion runs, and the plate Cf
-    of both solves is compared with the inverted-beta solution.  out_path (a
-    JSON) is written after each stage, and an .npz beside it holds the wall
-    Cf arrays."""
+    of both solves is compared with the inverted-beta solution and with the
+    target Cf the inversion aims for (max and mean over the plate faces).
+    out_path (a JSON) is written after each stage, and an .npz beside it holds
+    the wall Cf arrays."""
     import torch
     from . import case as C
     from . import inversion as inv
@@ -255,11 +256,13 @@ def heldout(ni: int, nj: int, iters: int, study: str, out_path: str | None, log=
     eq.mlp_enable(False)
     eq.close()
     summary, arrays = inv.run_case(re_l, ang, ni, nj, max_iter=iters, log=log)
-    cf_inv = arrays["cf_inv"]
-    err = lambda cf: float(np.abs((cf - cf_inv)[mask] / cf_inv[mask]).max())
+    cf_inv, cf_t = arrays["cf_inv"], arrays["cf_target"]
+    err = lambda cf, ref: np.abs((cf - ref)[mask] / ref[mask])
     out["inversion"] = summary
-    out["plain_sa"]["cf_err_vs_inverted"] = err(cfs["plain_sa"])
-    out["learned"]["cf_err_vs_inverted"] = err(cfs["learned"])
+    for label in ("plain_sa", "learned"):
+        e_inv, e_t = err(cfs[label], cf_inv), err(cfs[label], cf_t)
+        out[label].update(cf_err_vs_inverted=float(e_inv.max()), cf_err_vs_target=float(e_t.max()),
+                          cf_err_vs_target_mean=float(e_t.mean()))
     log("[heldout] " + json.dumps(out))
     save()
     if out_path:
