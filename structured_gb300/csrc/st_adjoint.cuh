@@ -150,14 +150,13 @@ __device__ inline void roe_rev(const RoeTape& t, const double* fb, double* bl, d
         hav_ += tmp;
         uav_ -= tmp * t.uav; vav_ -= tmp * t.vav;
     }
-    double rat_ = 0, rati_ = 0, hrht_ = 0, hlft_ = 0;
-    rat_ += (hav_ * t.hrht + vav_ * vrht + uav_ * urht) * t.rati;
-    hrht_ += hav_ * t.rat * t.rati; hlft_ += hav_ * t.rati;
-    vrht_ += vav_ * t.rat * t.rati; vlft_ += vav_ * t.rati;
-    urht_ += uav_ * t.rat * t.rati; ulft_ += uav_ * t.rati;
-    rati_ += hav_ * (t.rat * t.hrht + t.hlft) + vav_ * (t.rat * vrht + vlft) + uav_ * (t.rat * urht + ulft);
-    rat_ += rav_ * rlft; rlft_ += rav_ * t.rat;
-    rat_ += -rati_ * t.rati * t.rati;
+    // x_av = (rat x_rht + x_lft) rati with rati = 1 / (rat + 1): d x_av / d rat = rati (x_rht - x_av)
+    const double w = t.rat * t.rati;
+    double hrht_ = hav_ * w, hlft_ = hav_ * t.rati;
+    vrht_ += vav_ * w; vlft_ += vav_ * t.rati;
+    urht_ += uav_ * w; ulft_ += uav_ * t.rati;
+    const double rat_ = t.rati * (hav_ * (t.hrht - t.hav) + vav_ * (vrht - t.vav) + uav_ * (urht - t.uav)) + rav_ * rlft;
+    rlft_ += rav_ * t.rat;
     double rlfti_ = 0, rrhti_ = 0;
     {
         const double tmp = rat_ * 0.5 * t.irat;

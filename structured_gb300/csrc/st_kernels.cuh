@@ -266,8 +266,9 @@ __global__ void __launch_bounds__(256) k_limiter(DevCase c, const T* __restrict_
                 lim[lim_off(c, dir, LIM_SL, idx) + k] = ph * tl;
                 lim[lim_off(c, dir, LIM_SR, idx) + k] = ph * tr;
                 if (ADJ) {
-                    const T dfa = (0.75 * fb - ph * (3.0 * fb - 4.0 * (fb - fa))) * inv;
-                    const T dfb = (0.75 * fa - ph * (3.0 * fa + 4.0 * (fb - fa))) * inv;
+                    // d phi / d d-, d+: 3 d+ - 4 (d+ - d-) = 4 d- - d+, 3 d- + 4 (d+ - d-) = 4 d+ - d-
+                    const T dfa = (0.75 * fb - ph * (4.0 * fa - fb)) * inv;
+                    const T dfb = (0.75 * fa - ph * (4.0 * fb - fa)) * inv;
                     lim[lim_off(c, dir, LIM_AM, idx) + k] = ph * THM + tl * dfa;
                     lim[lim_off(c, dir, LIM_AP, idx) + k] = ph * THP + tl * dfb;
                     lim[lim_off(c, dir, LIM_BM, idx) + k] = ph * THP + tr * dfa;
