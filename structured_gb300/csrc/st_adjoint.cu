@@ -1,6 +1,7 @@
 // C ABI of the hand-written discrete adjoint: launch sequence of the reverse
 // passes in st_adjoint.cuh.
 #include <algorithm>
+#include <cstring>
 
 #include "st_adjoint.cuh"
 #include "st_context.h"
@@ -18,6 +19,10 @@ int alloc_d(T** p, size_t n) {
     return ST_OK;
 }
 
+// Grids whose host-buffer VJP runs the gather in bands with the boundary ring
+// after it: at least eight bands' worth of cells and eight cells a side.
+bool ringed_grid(const st_ctx* x) { return x->c.ni - 1 >= 8 && x->c.nj - 1 >= 8 && x->ncell >= 2 * 65536; }
+
 int ensure(st_ctx* x) {
     if (x->Pbar) return ST_OK;
     const int nq = x->nq;
@@ -31,6 +36,14 @@ int ensure(st_ctx* x) {
     if (rc == ST_OK) rc = alloc_d(&x->psi_tmp, x->ncell * nq);
     if (rc == ST_OK) rc = alloc_d(&x->outq_tmp, x->ncell * nq);
     if (rc == ST_OK) rc = alloc_d(&x->outb_tmp, x->ncell);
+    if (rc == ST_OK && ringed_grid(x)) {
+        const size_t nr = ring_cells(x->c.ni - 1, x->c.nj - 1) * nq;
+        rc = alloc_d(&x->ring_dev, nr);
+        if (rc == ST_OK) {
+            const cudaError_t e = cudaHostAlloc((void**)&x->ring_host, nr * sizeof(double), cudaHostAllocDefault);
+            if (e != cudaSuccess) rc = stx::cuda_fail(e, "cudaHostAlloc (boundary ring)");
+        }
+    }
     if (rc) return rc;
     ST_CUDA(cudaMemsetAsync(x->srec, 0, x->ncell * SRW * 8, x->stream));
     return ST_OK;
@@ -89,25 +102,56 @@ int launch_fused(st_ctx* x, const double* psi, double* rhs, double* outq, double
             if (rc) return rc;
         }
     }
-    k_gather<NQ, ORDER><<<grid_for(x->npad), 256, 0, s>>>(dc, x->P, x->arec_i, x->arec_j, x->srec, x->Pbar);
-    stx::mark(x, "k_gather");
-    {
-        const unsigned gr = (unsigned)((2 * (x->c.ni + 1) + 2 * (x->c.nj - 1) + 255) / 256);
-        const unsigned gb = (unsigned)((std::max(x->c.ni, x->c.nj) + 1 + 255) / 256);
+    const unsigned gr = (unsigned)((2 * (x->c.ni + 1) + 2 * (x->c.nj - 1) + 255) / 256);
+    const unsigned gb = (unsigned)((std::max(x->c.ni, x->c.nj) + 1 + 255) / 256);
+    auto bc_reverse = [&]() {
         if (dc.viscous) k_bc_adj_mu<NQ><<<gr, 256, 0, s>>>(dc, x->P, x->Pbar);
         for (int b = (int)x->bcs.size() - 1; b >= 0; b--) {
             k_bc_adj_one<NQ><<<gb, 256, 0, s>>>(dc, x->P, x->tape, x->Pbar, b, 0);
             if (x->bcs[b].type == ST_BC_WAKE) k_bc_adj_one<NQ><<<gb, 256, 0, s>>>(dc, x->P, x->tape, x->Pbar, b, 1);
         }
-    }
-    stx::mark(x, "k_bc_adj");
-    {
+    };
+    if (x->hio.outq && x->ring_dev) {
+        // host-buffer call: the gather in bands of padded rows, each band's
+        // interior state products right behind it and on their way to the
+        // host while the next band gathers; the boundary ring, which the
+        // boundary reverse still changes, after that reverse, packed
+        const int nic = x->c.ni - 1, njc = x->c.nj - 1, nb = st_ctx::kBands;
+        const size_t rowp = (size_t)njc + 2;
+        for (int b = 0; b < nb; b++) {
+            const int r0 = (nic + 2) * b / nb, r1 = (nic + 2) * (b + 1) / nb;
+            k_gather<NQ, ORDER><<<grid_for((r1 - r0) * rowp), 256, 0, s>>>(dc, x->P, x->arec_i, x->arec_j, x->srec,
+                                                                          x->Pbar, r0 * rowp, r1 * rowp);
+            const size_t i0 = (size_t)std::max(r0, 1) - 1, i1 = (size_t)std::min(r1, nic + 1) - 1;
+            if (i1 > i0) {
+                k_prim_adj<NQ><<<grid_for((i1 - i0) * njc), 256, 0, s>>>(dc, x->q, x->P, x->Pbar, outq, i0 * njc,
+                                                                        i1 * njc, true);
+                const int rc = stx::copy_out(x, x->band_ev[b], x->hio.outq + i0 * njc * NQ, outq + i0 * njc * NQ,
+                                             (i1 - i0) * njc * NQ * 8);
+                if (rc) return rc;
+            }
+        }
+        stx::mark(x, "k_gather");
+        bc_reverse();
+        stx::mark(x, "k_bc_adj");
+        const size_t nr = ring_cells(nic, njc);
+        k_prim_adj_ring<NQ><<<grid_for(nr), 256, 0, s>>>(dc, x->q, x->P, x->Pbar, outq, x->ring_dev);
+        stx::mark(x, "k_prim_adj");
+        const int rc = stx::copy_out(x, x->xev[4], x->ring_host, x->ring_dev, nr * NQ * 8);
+        if (rc) return rc;
+        x->ring_pending = true;
+    } else {
+        k_gather<NQ, ORDER><<<grid_for(x->npad), 256, 0, s>>>(dc, x->P, x->arec_i, x->arec_j, x->srec, x->Pbar, 0,
+                                                            x->npad);
+        stx::mark(x, "k_gather");
+        bc_reverse();
+        stx::mark(x, "k_bc_adj");
         const int rc = stx::run_banded(x, x->hio.outq, outq, NQ, [&](size_t f, size_t l) {
             k_prim_adj<NQ><<<grid_for(l - f), 256, 0, s>>>(dc, x->q, x->P, x->Pbar, outq, f, l);
         });
         if (rc) return rc;
+        stx::mark(x, "k_prim_adj");
     }
-    stx::mark(x, "k_prim_adj");
     ST_LAUNCH_CHECK("residual/adjoint launch");
     return ST_OK;
 }
@@ -177,19 +221,31 @@ int host_vjp_enqueue(st_ctx* x, const double* psi_host, double* rhs_host, double
 // Host-buffer VJP (and residual): psi goes in on the copy stream while the
 // forward passes run, and the pipeline waits for it before its first read of
 // psi; the beta product and the residual go out on that stream as soon as
-// they are final, during the gather; k_prim_adj runs in bands whose outputs
-// go out while the next band computes.  Both streams are drained before the
-// call returns, on errors too, so the caller's buffers are free again.
+// they are final, during the gather.  The gather runs in bands, each followed
+// by k_prim_adj on the band's interior cells, whose state products go out
+// while the next band gathers; the boundary ring follows the boundary reverse
+// and is copied packed, then scattered into out_q_host here (small grids: the
+// gather whole, then k_prim_adj in bands).  Both streams are drained before
+// the call returns, on errors too, so the caller's buffers are free again.
 int host_vjp(st_ctx* x, const double* psi_host, double* rhs_host, double* outq_host, double* outb_host, int lhs,
              bool with_rhs) {
     int rc = ensure(x);
     if (rc) return rc;
+    x->ring_pending = false;
     rc = host_vjp_enqueue(x, psi_host, rhs_host, outq_host, outb_host, lhs, with_rhs);
     const cudaError_t e1 = cudaStreamSynchronize(x->xfer);
     const cudaError_t e2 = cudaStreamSynchronize(x->stream);
+    const bool ring = x->ring_pending;
+    x->ring_pending = false;
     if (rc) return rc;
     if (e1 != cudaSuccess) return stx::cuda_fail(e1, "cudaStreamSynchronize (copy stream)");
     if (e2 != cudaSuccess) return stx::cuda_fail(e2, "cudaStreamSynchronize");
+    if (ring) {  // the boundary ring of the state product into its place in out_q_host
+        const int nic = x->c.ni - 1, njc = x->c.nj - 1, nq = x->nq;
+        const size_t nr = ring_cells(nic, njc);
+        for (size_t r = 0; r < nr; r++)
+            std::memcpy(outq_host + ring_cell(nic, njc, r) * nq, x->ring_host + r * nq, nq * sizeof(double));
+    }
     return ST_OK;
 }
 }  // namespace

@@ -652,10 +652,10 @@ __global__ void __launch_bounds__(256) k_cell_res(DevCase c, const double* __res
 template <int NQ, int ORDER>
 __global__ void __launch_bounds__(256) k_gather(DevCase c, const double* __restrict__ P, const double* __restrict__ ai,
                                                 const double* __restrict__ aj, const double* __restrict__ srec,
-                                                double* __restrict__ Pbar) {
-    const size_t n = (size_t)(c.nic + 2) * (c.njc + 2);
+                                                double* __restrict__ Pbar, size_t first, size_t n) {
     const int slot[5] = {P_RHO, P_U, P_V, P_P, P_NUT};
-    for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += (size_t)gridDim.x * blockDim.x) {
+    for (size_t idx = first + (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n;
+         idx += (size_t)gridDim.x * blockDim.x) {
         const int ip = (int)(idx / (c.njc + 2)), jp = (int)(idx % (c.njc + 2));
         double acc[NP];
 #pragma unroll
@@ -1007,47 +1007,92 @@ static __global__ void __launch_bounds__(256) k_tape_ring(DevCase c, const doubl
 
 // R6: primitives -> conserved adjoint per physical cell (reverse of k_prim).
 template <int NQ>
+__device__ inline void prim_adj_cell(const DevCase& c, const double* __restrict__ q, const double* __restrict__ P,
+                                     const double* __restrict__ Pbar, double* __restrict__ Qb_out, size_t idx) {
+    const int i = (int)(idx / c.njc), j = (int)(idx % c.njc);
+    const double* Q = q + idx * NQ;
+    const double* p = P + pidx(c, i + 1, j + 1);
+    const double* b = Pbar + pidx(c, i + 1, j + 1);
+    const double rho = Q[0], ri = nr_rcp(rho), u = p[P_U], v = p[P_V];
+    double rhob = b[P_RHO], ub = b[P_U], vb = b[P_V], pb = b[P_P], Tb = b[P_T], nutb = b[P_NUT], mub = b[P_MU];
+    if (c.viscous) {
+        const double mu = p[P_MU];
+        if (NQ == 5 && p[P_NUT] >= 0.0) {  // mu_t = 0 for nut < 0
+            const double s = rho * p[P_NUT];
+            const double chi = s * nr_rcp(mu), chi3 = chi * chi * chi, iden = nr_rcp(chi3 + SA_CV1_3);
+            const double f = chi3 * iden, fp = 3.0 * chi * chi * SA_CV1_3 * (iden * iden);
+            const double ds = f + chi * fp;
+            rhob += b[P_MUT] * ds * p[P_NUT];
+            nutb += b[P_MUT] * ds * rho;
+            mub += b[P_MUT] * (-chi * chi * fp);
+        }
+        const double iT = nr_rcp(p[P_T]);
+        const double dmu = c.law == 1 ? mu * (1.5 * iT - nr_rcp(p[P_T] + c.suth_S)) : (2.0 / 3.0) * mu * iT;
+        Tb += mub * dmu;
+    }
+    const double iR = c.iR;
+    pb += Tb * ri * iR;
+    double rib = Tb * p[P_P] * iR;
+    double Qb[5] = {0, 0, 0, 0, 0};
+    if (NQ == 5) { Qb[4] = nutb * ri; rib += nutb * Q[4]; }
+    Qb[3] = pb * GM1;
+    rhob += -0.5 * (u * u + v * v) * GM1 * pb;
+    ub += -rho * GM1 * u * pb;
+    vb += -rho * GM1 * v * pb;
+    Qb[2] = vb * ri; rib += vb * Q[2];
+    Qb[1] = ub * ri; rib += ub * Q[1];
+    rhob += -rib * ri * ri;
+    Qb[0] = rhob;
+#pragma unroll
+    for (int k = 0; k < NQ; k++) Qb_out[k] = Qb[k];
+}
+
+// Boundary ring of the physical cells: the two outermost rows and columns,
+// whose primitive adjoints the boundary reverse still changes after the
+// gather.  Ring index r: rows 0, 1 (r < 2 njc), rows nic-2, nic-1 (< 4 njc),
+// then columns 0, 1, njc-2, njc-1 of rows 2 .. nic-3.  Needs nic, njc >= 4.
+__host__ __device__ inline size_t ring_cells(int nic, int njc) { return 4 * (size_t)njc + 4 * (size_t)(nic - 4); }
+__host__ __device__ inline size_t ring_cell(int nic, int njc, size_t r) {
+    if (r < 2 * (size_t)njc) return r;
+    if (r < 4 * (size_t)njc) return (size_t)(nic - 2) * njc + (r - 2 * (size_t)njc);
+    const size_t rr = r - 4 * (size_t)njc;
+    const int i = 2 + (int)(rr / 4), k = (int)(rr % 4);
+    const int j = k < 2 ? k : njc - 4 + k;
+    return (size_t)i * njc + j;
+}
+__host__ __device__ inline bool in_ring(int nic, int njc, size_t idx) {
+    const int i = (int)(idx / njc), j = (int)(idx % njc);
+    return i < 2 || i >= nic - 2 || j < 2 || j >= njc - 2;
+}
+
+// The pass over the cells [first, n); skip_ring leaves the boundary ring out
+// (the host-buffer call runs it after the boundary reverse).
+template <int NQ>
 __global__ void __launch_bounds__(256) k_prim_adj(DevCase c, const double* __restrict__ q, const double* __restrict__ P,
                                                   const double* __restrict__ Pbar, double* __restrict__ out,
-                                                  size_t first, size_t n) {
+                                                  size_t first, size_t n, bool skip_ring = false) {
     for (size_t idx = first + (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n;
          idx += (size_t)gridDim.x * blockDim.x) {
-        const int i = (int)(idx / c.njc), j = (int)(idx % c.njc);
-        const double* Q = q + idx * NQ;
-        const double* p = P + pidx(c, i + 1, j + 1);
-        const double* b = Pbar + pidx(c, i + 1, j + 1);
-        const double rho = Q[0], ri = nr_rcp(rho), u = p[P_U], v = p[P_V];
-        double rhob = b[P_RHO], ub = b[P_U], vb = b[P_V], pb = b[P_P], Tb = b[P_T], nutb = b[P_NUT], mub = b[P_MU];
-        if (c.viscous) {
-            const double mu = p[P_MU];
-            if (NQ == 5 && p[P_NUT] >= 0.0) {  // mu_t = 0 for nut < 0
-                const double s = rho * p[P_NUT];
-                const double chi = s * nr_rcp(mu), chi3 = chi * chi * chi, iden = nr_rcp(chi3 + SA_CV1_3);
-                const double f = chi3 * iden, fp = 3.0 * chi * chi * SA_CV1_3 * (iden * iden);
-                const double ds = f + chi * fp;
-                rhob += b[P_MUT] * ds * p[P_NUT];
-                nutb += b[P_MUT] * ds * rho;
-                mub += b[P_MUT] * (-chi * chi * fp);
-            }
-            const double iT = nr_rcp(p[P_T]);
-            const double dmu = c.law == 1 ? mu * (1.5 * iT - nr_rcp(p[P_T] + c.suth_S)) : (2.0 / 3.0) * mu * iT;
-            Tb += mub * dmu;
-        }
-        const double iR = c.iR;
-        pb += Tb * ri * iR;
-        double rib = Tb * p[P_P] * iR;
-        double Qb[5] = {0, 0, 0, 0, 0};
-        if (NQ == 5) { Qb[4] = nutb * ri; rib += nutb * Q[4]; }
-        Qb[3] = pb * GM1;
-        rhob += -0.5 * (u * u + v * v) * GM1 * pb;
-        ub += -rho * GM1 * u * pb;
-        vb += -rho * GM1 * v * pb;
-        Qb[2] = vb * ri; rib += vb * Q[2];
-        Qb[1] = ub * ri; rib += ub * Q[1];
-        rhob += -rib * ri * ri;
-        Qb[0] = rhob;
+        if (skip_ring && in_ring(c.nic, c.njc, idx)) continue;
+        prim_adj_cell<NQ>(c, q, P, Pbar, out + idx * NQ, idx);
+    }
+}
+
+// The boundary ring's pass: writes out and, packed by ring index, pack.
+template <int NQ>
+__global__ void __launch_bounds__(256) k_prim_adj_ring(DevCase c, const double* __restrict__ q,
+                                                       const double* __restrict__ P, const double* __restrict__ Pbar,
+                                                       double* __restrict__ out, double* __restrict__ pack) {
+    const size_t nr = ring_cells(c.nic, c.njc);
+    for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < nr; r += (size_t)gridDim.x * blockDim.x) {
+        const size_t idx = ring_cell(c.nic, c.njc, r);
+        double v[NQ];
+        prim_adj_cell<NQ>(c, q, P, Pbar, v, idx);
 #pragma unroll
-        for (int k = 0; k < NQ; k++) out[idx * NQ + k] = Qb[k];
+        for (int k = 0; k < NQ; k++) {
+            out[idx * NQ + k] = v[k];
+            pack[r * NQ + k] = v[k];
+        }
     }
 }
 

@@ -723,13 +723,15 @@ int st_create(const st_case* c, const double* xv, const double* yv, int device, 
 int st_destroy(st_ctx* x) {
     if (!x) return ST_OK;
     if (x->stream) cudaStreamSynchronize(x->stream);
+    if (x->xfer) cudaStreamSynchronize(x->xfer);
     double* bufs[] = {x->q, x->rhs, x->beta, x->P, x->lim, x->Fi, x->Fj, x->Gi, x->Gj, x->vol_d, x->ivol_d,
                       x->geo_i, x->geo_j, x->wd, x->nchi_d, x->neta_d, x->dsmin_d, x->dt, x->norm_part, x->norm_out,
                       x->cf, x->wall_dx_d, x->Pbar, x->srec, x->arec_i, x->arec_j, x->psi_tmp,
                       x->outq_tmp, x->outb_tmp, x->tape, x->jac, x->jac1, x->kv, x->kzb, x->kz, x->kw, x->kr, x->kh, x->kpart, x->dq, x->qsave,
                       x->qtmp, x->wpart[0], x->wpart[1], x->wpart[2], x->wpart1[0], x->wpart1[1], x->wpart1[2],
-                      x->wallg, x->strip_jac_d, x->strip_dt_d, x->strip_inv_d, x->strip_res_d};
+                      x->wallg, x->strip_jac_d, x->strip_dt_d, x->strip_inv_d, x->strip_res_d, x->ring_dev};
     for (double* b : bufs) if (b) cudaFree(b);
+    if (x->ring_host) cudaFreeHost(x->ring_host);
     for (int* m : x->pmask_d) if (m) cudaFree(m);
     if (x->strip_cells_d) cudaFree(x->strip_cells_d);
     st::dual* dbufs[] = {x->qd, x->Pd, x->limd, x->Fdi, x->Fdj, x->Gdi, x->Gdj, x->rhsd, x->betad};

@@ -90,14 +90,20 @@ struct st_ctx {
     // only during such a call.  The pipeline waits on hio.psi_ready before
     // its first read of psi; it queues the copy of each output to its host
     // destination as soon as the output is final; and its last per-cell pass
-    // (k_cell, k_prim_adj) runs in bands, each band's output copied while
-    // the next band computes.
+    // (k_cell; the gather with k_prim_adj behind it) runs in bands, each
+    // band's output copied while the next band computes.
     struct HostIO {
         cudaEvent_t psi_ready = nullptr;
         double *rhs = nullptr, *outq = nullptr, *outb = nullptr;
     } hio;
     cudaStream_t xfer = nullptr;
-    cudaEvent_t xev[4] = {nullptr, nullptr, nullptr, nullptr};
+    cudaEvent_t xev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    // the host-buffer VJP's boundary ring of the state product (the two
+    // outermost rows and columns, which the boundary reverse changes after
+    // the gather), packed on the device and copied to page-locked host
+    // memory; ring_pending: the call still has to scatter it into place
+    double *ring_dev = nullptr, *ring_host = nullptr;
+    bool ring_pending = false;
     static constexpr int kBands = 8;
     cudaEvent_t band_ev[kBands] = {};
     // per-launch profiling (st_profile_pipeline): an event after each launch
